@@ -1,0 +1,191 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Run in a container where the reference checkout is present:
+
+    python tests/golden/make_golden.py /root/reference
+
+It imports the reference's ``dens.py`` and ``plot2d.py`` directly (their
+missing third-party modules -- ``past.utils``, ``tqdm`` progress bars and
+``matplotlib`` -- are replaced by small stubs that do not touch the
+arithmetic), runs ``dens.compute_sf`` on small seeded systems and
+``plot2d.Plot_Ewald_Sphere_Correction`` on the resulting ``kgridplt``, and
+saves inputs and outputs as compressed npz files.  Nothing is written into
+the reference tree (``sys.dont_write_bytecode``).
+
+Fixtures:
+  gauss_*.npz  -- inputs of ``dens.compute_sf`` and all six saved arrays.
+  ewald_*.npz  -- ``kgridplt``, wavelength and the three Ewald slices as
+                  recorded from the reference's ``contourf`` calls.
+  hist_edges.npz -- ``numpy.histogramdd`` on positions placed on and around
+                  bin edges (pins the binning semantics the CUDA deposit
+                  must match on numpy versions other than the one here).
+"""
+from __future__ import annotations
+
+import contextlib
+import io
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _install_stubs():
+    sys.dont_write_bytecode = True
+    past = types.ModuleType("past")
+    pu = types.ModuleType("past.utils")
+
+    def old_div(a, b):
+        if isinstance(a, (int, np.integer)) and isinstance(b, (int, np.integer)):
+            return a // b
+        return a / b
+    pu.old_div = old_div
+    past.utils = pu
+    sys.modules["past"] = past
+    sys.modules["past.utils"] = pu
+
+    calls = []
+
+    class _Rec:
+        def __getattr__(self, name):
+            def f(*a, **k):
+                calls.append((name, a, k))
+            return f
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    rec = _Rec()
+    for name in ("figure", "suptitle", "xlabel", "ylabel", "contourf", "savefig", "clf",
+                 "xlim", "ylim", "colorbar", "plot", "title", "close", "tight_layout"):
+        setattr(plt, name, getattr(rec, name))
+    ticker = types.ModuleType("matplotlib.ticker")
+    widgets = types.ModuleType("matplotlib.widgets")
+    widgets.Slider = widgets.Button = widgets.RadioButtons = object
+    mpl.pyplot, mpl.ticker, mpl.widgets = plt, ticker, widgets
+    mpl.rc = lambda *a, **k: None
+    sys.modules.update({"matplotlib": mpl, "matplotlib.pyplot": plt,
+                        "matplotlib.ticker": ticker, "matplotlib.widgets": widgets})
+    return calls
+
+
+class _Quiet:
+    def __init__(self, it, *a, **k):
+        self.it = it
+
+    def __iter__(self):
+        return iter(self.it)
+
+
+def gauss_cases():
+    rng = np.random.default_rng(20261203)
+    cases = {}
+
+    # orthorhombic, per-frame boxes (rescale), atoms on 0 / L / outside (wrap)
+    T, N = 2, 40
+    L = np.array([[12.0, 10.0, 8.0], [12.3, 9.8, 8.1]])
+    r = rng.uniform(0.0, 1.0, (T, N, 3)) * L[:, None, :]
+    r[0, 0] = [0.0, 0.0, 0.0]
+    r[0, 1] = L[0]
+    r[1, 2] = [-0.3, 10.2, 4.0]
+    r[1, 3] = [12.5, -0.01, 8.05]
+    typ = np.array((["O", "H", "H", "C", "N"] * 8)[:N], dtype=object)
+    cases["gauss_ortho"] = dict(r=r, L=L, typ=typ, ucell=np.eye(3), Sres=0.6)
+
+    # monoclinic cell (theta = 120 deg, main_gromacs.py:79-80), three frames
+    T, N = 3, 36
+    th = 120 * np.pi / 180.0
+    ucell = np.array([[1, 0, 0], [np.cos(th), np.sin(th), 0], [0, 0, 1]])
+    L = np.array([[9.0, 9.0, 11.0], [9.1, 8.9, 11.2], [8.95, 9.05, 10.9]])
+    r = rng.uniform(0.0, 1.0, (T, N, 3)) * L[:, None, :]
+    typ = np.array((["C", "O", "H", "H"] * 9)[:N], dtype=object)
+    cases["gauss_tcl"] = dict(r=r, L=L, typ=typ, ucell=ucell, Sres=0.7)
+
+    # atoms packed near the 8 corners: exercises the corner fold quirk
+    T, N = 1, 24
+    L = np.array([[7.0, 8.0, 9.0]])
+    corners = np.array([[a, b, c] for a in (0, 1) for b in (0, 1) for c in (0, 1)], float)
+    r = np.empty((T, N, 3))
+    for j in range(N):
+        c = corners[j % 8]
+        d = rng.uniform(0.05, 0.6, 3)
+        r[0, j] = np.where(c > 0, L[0] - d, d)
+    typ = np.array((["O", "N", "C"] * 8)[:N], dtype=object)
+    cases["gauss_corner"] = dict(r=r, L=L, typ=typ, ucell=np.eye(3), Sres=0.5)
+    return cases
+
+
+def hist_edges_case():
+    rng = np.random.default_rng(7)
+    L = np.array([2.5, 3.1, 1.7])
+    dims = np.array([16, 20, 10])
+    pts = [rng.uniform(0, 1, (200, 3)) * L]
+    for a in range(3):
+        e = np.linspace(0.0, L[a], dims[a] + 1)
+        p = rng.uniform(0, 1, (len(e), 3)) * L
+        p[:, a] = e
+        pts.append(p)
+        p2 = p.copy()
+        p2[:, a] = np.nextafter(e, -np.inf)
+        pts.append(p2)
+        p3 = p.copy()
+        p3[:, a] = np.nextafter(e, np.inf)
+        pts.append(p3)
+    extra = np.array([[0.0, 0.0, 0.0], L, [-0.0, 1.0, 1.0], [-1e-12, 1.0, 1.0],
+                      [L[0] + 1e-12, 1.0, 1.0], [np.nan, 1.0, 1.0], [1.0, np.inf, 1.0]])
+    pts.append(extra)
+    pos = np.concatenate(pts)
+    w = rng.choice([1, 6, 7, 8], len(pos)).astype(np.int32)
+    H, _ = np.histogramdd(pos, bins=dims, range=[(0, L[i]) for i in range(3)], weights=w.astype(float))
+    pos32 = pos.astype(np.float32)
+    H32, _ = np.histogramdd(pos32, bins=dims, range=[(0, L[i]) for i in range(3)], weights=w.astype(float))
+    F = np.fft.rfftn(H)
+    return dict(pos=pos, pos32=pos32, weights=w, L=L, dims=dims, grid=H.astype(np.int32),
+                grid32=H32.astype(np.int32), sf=(F.real ** 2 + F.imag ** 2))
+
+
+def main(ref):
+    calls = _install_stubs()
+    sys.path.insert(0, ref)
+    import dens
+    import plot2d
+    dens.tqdm.tqdm = _Quiet
+    rad = dens.load_radii(os.path.join(ref, "radii.txt"))
+    tmp = tempfile.mkdtemp()
+    for name, c in gauss_cases().items():
+        r_in = c["r"].copy()
+        L_in = c["L"].copy()
+        out = os.path.join(tmp, name)
+        with contextlib.redirect_stdout(io.StringIO()):
+            dens.compute_sf(c["r"], c["L"], c["typ"], out, rad, c["ucell"], c["Sres"])
+        z = np.load(out + ".npz")
+        names = sorted(set(c["typ"]))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), r=r_in, L_in=L_in,
+                            r_after=c["r"], typ=c["typ"].astype(str), ucell=c["ucell"],
+                            Sres=c["Sres"], rad_names=np.array(names),
+                            rad_nel=np.array([rad[n][0] for n in names]),
+                            rad_sigma=np.array([rad[n][1] for n in names]),
+                            **{"out_" + k: z[k] for k in z.files})
+        print(name, {k: z[k].shape for k in z.files})
+
+    plot2d.path = tmp + os.sep
+    for name, lam in (("gauss_ortho", 1.54), ("gauss_tcl", 1.54), ("gauss_corner", 0.9)):
+        D = np.load(os.path.join(HERE, name + ".npz"))["out_kgridplt"]
+        del calls[:]
+        with contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
+            plot2d.Plot_Ewald_Sphere_Correction(D, lam)
+        cf = [c for c in calls if c[0] == "contourf"]
+        # figures 1, 3, 5 plot the linear slices xy, xz, yz (plot2d.py:280-324)
+        xy, xz, yz = cf[0][1][2], cf[2][1][2], cf[4][1][2]
+        np.savez_compressed(os.path.join(HERE, "ewald_" + name.split("_", 1)[1] + ".npz"),
+                            D=D, wavelength=lam, xy=xy, xz=xz, yz=yz)
+        print("ewald", name, xy.shape, xz.shape, yz.shape, np.isnan(xy).sum())
+
+    np.savez_compressed(os.path.join(HERE, "hist_edges.npz"), **hist_edges_case())
+    print("hist_edges done")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
