@@ -1,0 +1,440 @@
+"""Benchmark: frames/s of the structure-factor chain at 256x256x128, 200k atoms.
+
+Workload (one step): the seeded columnar system -- 200,000 atoms in a
+16.0 x 13.856 x 8.0 nm box, 100 frames of float32 positions (320 MB as
+float4, more than L2) -- through histogram deposit -> R2C FFT -> |F|^2 ->
+FP64 frame sum, then get_dplot and the Ewald slices at lambda = 0.154 nm.
+
+  value       frames/s of the batched chain captured once in a CUDA graph
+              and replayed per step, inputs resident in HBM.
+  e2e         the same through the public API from pinned HOST buffers:
+              H2D of the step's positions (streamed on a side stream) and
+              D2H of sf inside the timed region.
+  roofline    the dominant kernel, timed live with CUDA events over a pass
+              of the same workload driven stage by stage.
+  cpu_baseline the numpy oracle (histogramdd + rfftn, one core) on a bounded
+              sample of frames of the same workload.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+N>1 runs under torchrun: every rank processes its own trajectory (frames
+shard with no exchange until one FP64 sum of sf per step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "md-structure-factor_gb300"))
+sys.path.insert(0, ROOT)
+
+DIMS = (256, 256, 128)
+N_ATOMS = 200_000
+FRAMES = 100
+BOX = (16.0, 13.856, 8.0)
+WAVELENGTH = 0.154
+METRIC = "frames/s at 256^2x128 grid, 200k atoms (batched, graph-captured hist->FFT->|F|^2->FP64 sum)"
+WORKLOAD = "columnar 200k atoms, 16.0x13.856x8.0 nm, 256x256x128 grid, 100 frames/step, f32 positions, Ewald lambda=0.154 nm"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes_per_frame(n_atoms=N_ATOMS, dims=DIMS):
+    V = dims[0] * dims[1] * dims[2]
+    Vh = dims[0] * dims[1] * (dims[2] // 2 + 1)
+    return 16 * n_atoms + 8 * V + 16 * Vh
+
+
+class Clocks:
+    """nvidia-smi sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.index = index
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except Exception:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_port_baseline(pos, box, w, budget_s=12.0, min_frames=2):
+    """Oracle port (numpy histogramdd + rfftn + |F|^2, FP64) on one core."""
+    from oracle import hist as ohist
+    sf = np.zeros((DIMS[0], DIMS[1], DIMS[2] // 2 + 1))
+    t0 = time.perf_counter()
+    n = 0
+    while n < pos.shape[0] and (n < min_frames or time.perf_counter() - t0 < budget_s):
+        sf += ohist.power(ohist.hist_grid(pos[n], box, w, DIMS))
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
+            "sample": f"{n} frames of the same workload, numpy histogramdd + numpy.fft.rfftn + |F|^2 + FP64 sum, "
+                      f"single thread ({dt:.1f} s)"}
+
+
+def _ref_worker(args):
+    seed, frames = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from mdsf import synth
+    from oracle import hist as ohist
+    pos, box, w = synth.columnar(n_atoms=N_ATOMS, box=BOX, frames=frames, seed=seed)
+    t0 = time.perf_counter()
+    sf = np.zeros((DIMS[0], DIMS[1], DIMS[2] // 2 + 1))
+    for t in range(frames):
+        sf += ohist.power(ohist.hist_grid(pos[t], box, w, DIMS))
+    return frames, time.perf_counter() - t0, float(sf[0, 0, 0])
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU method (the oracle port: the
+    reference is pure Python and cannot run on the GPU host) on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    frames_per_worker = 2
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_ref_worker, [(1000 + step * cores + i, frames_per_worker) for i in range(cores)])
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                times.append((sum(r[0] for r in res), dt))
+    frames = sum(t[0] for t in times)
+    total = sum(t[1] for t in times)
+    value = frames / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded columnar system)",
+            "config": {"workload": WORKLOAD, "sample_per_step": f"{frames_per_worker} frames x {cores} processes"},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": f"{frames_per_worker} frames per process per step, {cores} spawn processes, "
+                                       "numpy histogramdd + numpy.fft.rfftn + |F|^2 + FP64 sum (the reference has no "
+                                       "GPU-host-runnable code: it is pure Python and absent on the GPU host)"},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--tile-w", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import mdsf
+    from mdsf import synth
+    from mdsf._lib import c_p, call
+    from mdsf.api import _ptr
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    pos, box, w = synth.columnar(n_atoms=N_ATOMS, box=BOX, frames=FRAMES, seed=2 + 7919 * rank)
+    pos4_h = torch.from_numpy(synth.pack_float4(pos, w)).pin_memory()
+    pos4 = pos4_h.to(dev)
+    tuning = {}
+    if args.batch:
+        tuning["batch"] = args.batch
+    if args.variant:
+        tuning["variant"] = args.variant
+    if args.tile_w:
+        tuning["tile_w"] = args.tile_w
+    if not tuning:
+        from mdsf import tune
+        tuning = tune.lookup(DIMS) or {"batch": 8}
+    plan = mdsf.get_plan(DIMS, box, device=dev, **tuning)
+    st = torch.cuda.current_stream(dev)
+    sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=dev)
+    X, Y, Z = mdsf.plot_axes(plan.half_shape, box)
+    Xd, Yd, Zd = (torch.from_numpy(a).to(dev) for a in (X, Y, Z))
+    D = torch.empty((DIMS[0] - 2, DIMS[1] - 2, 2 * plan.nh - 3), dtype=torch.float64, device=dev)
+    ew = [torch.empty(s, dtype=torch.float64, device=dev) for s in
+          ((D.shape[0], D.shape[1]), (D.shape[0], D.shape[2]), (D.shape[1], D.shape[2]))]
+    K = 2.0 * np.pi / WAVELENGTH
+
+    def step_body():
+        sf.zero_()
+        sp = c_p(torch.cuda.current_stream(dev).cuda_stream)   # the capture stream inside graph capture
+        call("msf_hist_sf_f32", plan.handle, _ptr(pos4), N_ATOMS, FRAMES, c_p(0), 0, _ptr(sf), sp)
+        if world > 1:
+            dist.all_reduce(sf)
+        call("msf_sfplt", _ptr(sf), DIMS[0], DIMS[1], plan.nh, _ptr(D), sp)
+        call("msf_ewald", _ptr(D), D.shape[0], D.shape[1], D.shape[2], _ptr(Xd), _ptr(Yd), _ptr(Zd), K,
+             _ptr(ew[0]), _ptr(ew[1]), _ptr(ew[2]), sp)
+
+    batches = (FRAMES + plan.batch - 1) // plan.batch
+    launches_per_step = batches * (3 if plan.variant == 1 else 4) + 2
+
+    # warm-up (also primes one-time kernel attributes before graph capture)
+    for _ in range(2):
+        step_body()
+    torch.cuda.synchronize()
+    graph = None
+    if world == 1:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step_body()
+        run = graph.replay
+    else:
+        run = step_body
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms
+
+    with Clocks(local) as clk:
+        ms = timed(run, args.steps)
+    clocks = clk.summary()
+    ms_per_step = ms / args.steps
+    value = FRAMES * world * args.steps / (ms / 1000.0)
+    # correctness guard on the timed output: DC term = (sum of weights)^2 per frame
+    dc = float(sf[0, 0, 0].item())
+    dc_ref = FRAMES * world * float(np.sum(w, dtype=np.float64)) ** 2
+    assert abs(dc - dc_ref) < 1e-5 * dc_ref, (dc, dc_ref)
+
+    # ---- e2e: public API from pinned host buffers, D2H of sf in the timed region
+    sf_h = torch.empty(plan.half_shape, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning, stream_chunk=plan.batch * 4)
+        if world > 1:
+            dist.all_reduce(out)
+        sf_h.copy_(out, non_blocking=True)
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    ms_e2e = timed(e2e_step, args.steps)
+    e2e_value = FRAMES * world * args.steps / (ms_e2e / 1000.0)
+
+    # ---- roofline: each stage timed live with events around its launches
+    stage_ms = {1: [], 2: [], 4: []}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    sf.zero_()
+    sp = c_p(st.cuda_stream)
+    torch.cuda.synchronize()
+    for f0 in range(0, FRAMES, plan.batch):
+        k = min(plan.batch, FRAMES - f0)
+        p = c_p(pos4.data_ptr() + f0 * N_ATOMS * 16)
+        ev[0].record()
+        call("msf_hist_batch_stages", plan.handle, 1, 0, p, c_p(0), N_ATOMS, k, c_p(0), 0, _ptr(sf), sp)
+        ev[1].record()
+        call("msf_hist_batch_stages", plan.handle, 2, 0, p, c_p(0), N_ATOMS, k, c_p(0), 0, _ptr(sf), sp)
+        ev[2].record()
+        call("msf_hist_batch_stages", plan.handle, 4, 0, p, c_p(0), N_ATOMS, k, c_p(0), 0, _ptr(sf), sp)
+        ev[3].record()
+        torch.cuda.synchronize()
+        for s, (a, b) in zip((1, 2, 4), ((0, 1), (1, 2), (2, 3))):
+            stage_ms[s].append((ev[a].elapsed_time(ev[b]), k))
+    V = DIMS[0] * DIMS[1] * DIMS[2]
+    Vh = DIMS[0] * DIMS[1] * plan.nh
+    B = plan.batch
+    # compulsory bytes of each stage for one launch of `B` frames
+    stage_bytes = {
+        1: lambda k: 16 * N_ATOMS * k + 4 * V * k,                 # positions read, grid written
+        2: lambda k: 4 * V * k + 4 * V * k + 8 * Vh * k,            # grid read, grid zeroed, spectrum written
+        4: lambda k: 8 * Vh * k + 16 * Vh,                          # spectrum read, sf read + written
+    }
+    stage_names = {1: "k_hist_deposit", 2: "k_plane" if plan.variant == 1 else "k_zrows+k_ycols", 4: "k_xpower"}
+    totals = {s: sum(t for t, _ in v) for s, v in stage_ms.items()}
+    dom = max(totals, key=totals.get)
+    full = [(t, k) for t, k in stage_ms[dom] if k == B] or stage_ms[dom]
+    avg_ms = float(np.mean([t for t, _ in full]))
+    kfull = full[0][1]
+    achieved = stage_bytes[dom](kfull) / (avg_ms / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tj = json.load(f)
+        traffic = tj.get(stage_names[dom])
+    except Exception:
+        pass
+    chain_gbs = algorithmic_bytes_per_frame() * value / world / 1e9
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        extras = run_extras(mdsf, torch, dev, pos4, box, tuning, args)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_port_baseline(pos, box, w)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded columnar system (no dataset in the reference)",
+            "config": {"workload": WORKLOAD, "frames_per_step": FRAMES, "n_atoms": N_ATOMS, "grid": list(DIMS),
+                       "l2": "inputs larger than L2 (320 MB of float4 positions per step)",
+                       "arithmetic": "int32 grid (FP32 binning exact vs FP64 edges), FP32 FFT, FP64 frame sum",
+                       "tuning": plan.tuning(), "graph": world == 1, "parallelism": f"frames sharded x{world}"},
+            "roofline": {"bound": "hbm", "kernel": stage_names[dom], "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "frames_per_launch": kfull,
+                         "stage_ms_per_frame": {stage_names[s]: totals[s] / FRAMES for s in totals},
+                         "chain_algorithmic_gbs": chain_gbs, "chain_frac": chain_gbs / peak},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(pos4_h.numel() * 4),
+                    "d2h_bytes_per_step": int(sf_h.numel() * 8)},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "extras": extras,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
+    """Plain one-frame-per-launch path and the direct-sum gradient rate."""
+    from mdsf._lib import c_p, call
+    from mdsf.api import _ptr
+    out = {}
+    plan1 = mdsf.get_plan(DIMS, box, device=dev, batch=1)
+    sf = torch.zeros(plan1.half_shape, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def plain_step():
+        sp = c_p(st.cuda_stream)
+        for t in range(FRAMES):
+            call("msf_hist_sf_f32", plan1.handle, c_p(pos4.data_ptr() + t * N_ATOMS * 16), N_ATOMS, 1, c_p(0), 0,
+                 _ptr(sf), sp)
+            torch.cuda.synchronize()
+    plain_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_step()
+    torch.cuda.synchronize()
+    out["plain_frames_per_s"] = FRAMES / (time.perf_counter() - t0)
+    out["plain_note"] = "plan batch=1, one host call + synchronize per frame, no graph"
+
+    # direct sum: 20k atoms, 65,536 q, forward + adjoint, batch of 32 systems
+    rng = np.random.default_rng(4)
+    S_, N, M = 32, 20_000, 65_536
+    r = torch.from_numpy(rng.uniform(0, 6.0, (S_, N, 3)).astype(np.float32)).to(dev).requires_grad_(True)
+    f = torch.from_numpy(rng.choice(np.array([1, 6, 7, 8], np.float32), (S_, N))).to(dev)
+    d = rng.standard_normal((M, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    q = torch.from_numpy((d * rng.uniform(5, 15, (M, 1))).astype(np.float32)).to(dev)
+    target = torch.rand((S_, M), device=dev) * 100
+
+    def grad_eval():
+        S = mdsf.direct_sf(r, f, q)
+        loss = torch.mean((torch.log1p(S) - torch.log1p(target)) ** 2)
+        g, = torch.autograd.grad(loss, r)
+        return g
+    grad_eval()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 3
+    for _ in range(reps):
+        grad_eval()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    pairs = 2 * S_ * N * M
+    out["grad_evals_per_s"] = S_ / (ms / 1000.0)
+    out["grad_note"] = f"systems/s: forward+adjoint of {S_} systems x {N} atoms x {M} q per launch pair"
+    out["direct_pairs_per_s"] = pairs / (ms / 1000.0)
+    return out
+
+
+if __name__ == "__main__":
+    sys.exit(main())

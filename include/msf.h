@@ -1,0 +1,207 @@
+/*
+ * msf.h -- C ABI of libmsf.so, the GB300 (sm_103a) structure-factor library.
+ *
+ * The reference (joeyelk/MD-Structure-Factor) is pure Python: its hot path is
+ * the function dens.compute_sf(r, L, typ, out_filename, rad, ucell, Sres)
+ * (dens.py:166-346) and it has no FFI layer.  These entry points are what a
+ * binding of that path binds: each one names the reference lines it replaces.
+ *
+ * Conventions (every entry point):
+ *   - Every array argument is caller-owned DEVICE memory unless its name ends
+ *     in _host.  Nothing here allocates device memory or synchronises the
+ *     stream in a hot call; work is enqueued on `stream` (0 = legacy default).
+ *   - Return value: MSF_OK (0) or a negative MSF_E* status; msf_strerror()
+ *     turns it into text.  Errors detected on the GPU (e.g. an atom outside
+ *     the padded grid in Gaussian mode) are latched into the plan's device
+ *     status word and reported by msf_plan_status(), which synchronises.
+ *   - Plans are immutable after msf_plan_bind(); one plan may be used from
+ *     one stream at a time (its workspace is reused by every call).
+ *   - Grid arrays are C order (x slowest, z fastest).  The half spectrum has
+ *     shape (n0, n1, n2/2+1) like numpy.fft.rfftn; `sf` is FP64.
+ */
+#ifndef MSF_H_
+#define MSF_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* msf_stream_t; /* == cudaStream_t */
+
+enum {
+  MSF_OK = 0,
+  MSF_E_INVALID = -1,     /* bad argument (null pointer, bad size, bad flag) */
+  MSF_E_UNSUPPORTED = -2, /* size outside what the plan supports */
+  MSF_E_WORKSPACE = -3,   /* workspace missing or too small */
+  MSF_E_CUDA = -4,        /* a CUDA runtime call failed */
+  MSF_E_RANGE = -5,       /* an atom fell outside the grid (Gaussian mode) */
+  MSF_E_NOT_BOUND = -6,   /* plan used before msf_plan_bind */
+  MSF_E_TIMEOUT = -7,     /* a bounded device wait gave up */
+  MSF_E_TYPE = -8         /* unknown atom type index */
+};
+
+/* Flags for the deposit / chain calls. */
+enum {
+  MSF_WRAP = 1,          /* periodic wrap r<L?r:r-L; r>0?r:r+L first (dens.py:204-212) */
+  MSF_NO_ZERO_SF = 0     /* (default) accumulate into sf */
+};
+
+const char* msf_strerror(int status);
+int msf_version(void);          /* major*10000 + minor*100 + patch */
+
+/* ------------------------------------------------------------------ plans
+ * A plan fixes the grid (n0, n1, n2) and the number of frames processed per
+ * batch.  It owns host-side tables only.  msf_plan_workspace_bytes() tells
+ * how much device memory the caller must provide to msf_plan_bind(), which
+ * fills the twiddle/edge tables on the device and zeroes the density grids.
+ * Replaces: the grid set-up of dens.compute_sf (dens.py:181-189, 202,
+ * 237-263) -- dims are given directly instead of from a resolution.
+ */
+typedef struct msf_plan msf_plan;
+
+typedef struct msf_plan_desc {
+  int32_t n0, n1, n2;     /* grid; each in [2, 1024] */
+  int32_t batch;          /* frames per batch (>=1); 0 = default */
+  double box[3];          /* box edges L used for binning (mean box when frames are rescaled) */
+  int32_t variant;        /* FFT variant: 0 auto, 1 fused z+y plane, 2 split rows/cols */
+  int32_t tile_w;         /* columns per x-pass tile: 0 auto, else 4..32 */
+  int32_t rows_per_block; /* row pairs per z-pass block: 0 auto */
+  int32_t deposit_block;  /* threads per deposit block: 0 auto */
+} msf_plan_desc;
+
+int msf_plan_create(msf_plan** plan, const msf_plan_desc* desc);
+int msf_plan_destroy(msf_plan* plan);
+size_t msf_plan_workspace_bytes(const msf_plan* plan);
+int msf_plan_bind(msf_plan* plan, void* workspace, size_t workspace_bytes, msf_stream_t stream);
+/* Synchronises `stream`, returns and clears the device status word. */
+int msf_plan_status(msf_plan* plan, msf_stream_t stream);
+/* Effective tuning of a plan: variant, tile_w, rows_per_block, batch. */
+int msf_plan_query(const msf_plan* plan, int32_t out[8]);
+
+/* ------------------------------------------------ histogram deposit (a5)
+ * One frame -> int32 grid (n0, n1, n2): grid[b] += w_j where b is the
+ * numpy.histogramdd bin of atom j in [0, L) (last edge inclusive; atoms
+ * outside or NaN are dropped), bit-exact with numpy.  `grid` is ADDED to:
+ * zero it first for a plain histogram.
+ *   pos_w:  n_atoms float4 (x, y, z, w) with w an integer electron count.
+ *   scale:  NULL or 3 doubles: positions are multiplied by scale in FP64
+ *           before binning (the per-frame factor of dens.py:46-62).
+ * Stands in for the per-atom deposit of dens.py:283-311 (histogram form).
+ */
+int msf_hist_grid_f32(const msf_plan* plan, const void* pos_w, int64_t n_atoms,
+                      const double* scale, int32_t flags, int32_t* grid, msf_stream_t stream);
+/* float32 positions (n_atoms, 3) and int32 weights (n_atoms). */
+int msf_hist_grid_f32xyz(const msf_plan* plan, const float* pos, const int32_t* weights,
+                         int64_t n_atoms, const double* scale, int32_t flags, int32_t* grid,
+                         msf_stream_t stream);
+/* FP64 positions (n_atoms, 3) and int32 weights (n_atoms). */
+int msf_hist_grid_f64(const msf_plan* plan, const double* pos, const int32_t* weights,
+                      int64_t n_atoms, const double* scale, int32_t flags, int32_t* grid,
+                      msf_stream_t stream);
+
+/* ---------------------------------------- FFT power accumulate (a8, a9)
+ * sf += sum over the n_grids int32 grids g of |rfftn(g)|^2.  Replaces
+ * dens.py:313-318 (np.fft.rfftn, conj multiply, sf += dmag).  The grids are
+ * read-only here.
+ */
+int msf_power_accum_i32(msf_plan* plan, const int32_t* grids, int32_t n_grids, double* sf,
+                        msf_stream_t stream);
+/* Same for float32 real grids (used by the Gaussian path). */
+int msf_power_accum_f32(msf_plan* plan, const float* grids, int32_t n_grids, double* sf,
+                        msf_stream_t stream);
+
+/* ------------------------------------------ fused chain (a2, a4, a5, a8, a9)
+ * For frames t in [0, n_frames): deposit frame t's histogram, rfftn,
+ * |F|^2 and sf += -- the whole per-frame loop of dens.py:277-321 in
+ * histogram form, batched `batch` frames per pass.  sf is accumulated
+ * (the reference's undivided sum, dens.py:318).
+ *   pos_w:  (n_frames, n_atoms) float4 (x, y, z, w).
+ *   scale:  NULL or (n_frames, 3) doubles (per-frame rescale factors).
+ */
+int msf_hist_sf_f32(msf_plan* plan, const void* pos_w, int64_t n_atoms, int64_t n_frames,
+                    const double* scale, int32_t flags, double* sf, msf_stream_t stream);
+/* pos: (n_frames, n_atoms, 3) floats, weights: (n_atoms) int32. */
+int msf_hist_sf_f32xyz(msf_plan* plan, const float* pos, const int32_t* weights, int64_t n_atoms,
+                       int64_t n_frames, const double* scale, int32_t flags, double* sf,
+                       msf_stream_t stream);
+/* One batch (n_frames <= the plan's batch) of the chain, stage by stage, so
+ * that each stage can be timed or overlapped on its own: bit 1 = histogram
+ * deposit into the workspace grids, bit 2 = z/y FFT passes into the
+ * workspace spectra (zeroes the grids), bit 4 = x FFT pass, |F|^2 and
+ * sf +=.  layout: 0 = float4 (x, y, z, w), 1 = FP64 (N, 3) + int32
+ * weights, 2 = float32 (N, 3) + int32 weights.  Stages 1|2|4 together are
+ * one batch of msf_hist_sf_*. */
+int msf_hist_batch_stages(msf_plan* plan, int32_t stages, int32_t layout, const void* pos,
+                          const int32_t* weights, int64_t n_atoms, int32_t n_frames,
+                          const double* scale, int32_t flags, double* sf, msf_stream_t stream);
+/* pos: (n_frames, n_atoms, 3) doubles, weights: (n_atoms) int32. */
+int msf_hist_sf_f64(msf_plan* plan, const double* pos, const int32_t* weights, int64_t n_atoms,
+                    int64_t n_frames, const double* scale, int32_t flags, double* sf,
+                    msf_stream_t stream);
+
+/* ------------------------------------------------ Gaussian deposit (a6, a7)
+ * The reference's own density (dens.py:283-311): every atom adds
+ * Nel/sigma^3 * exp(-|ucell^T (r - g)|^2 / (2 sigma^2)) on the box
+ * [ir-A, ir+A) of the padded grid (ir = int(r/dr)), and the padding is
+ * folded onto the periodic cell as remap_grid_tcl does (dens.py:86-108),
+ * including its corner-block z destination (dens.py:107).  Computed in FP64
+ * and written to `grid` (FP64, n0*n1*n2, overwritten).  An atom whose box
+ * leaves the padded grid is skipped and latches MSF_E_RANGE (the reference
+ * raises a numpy broadcast error there).
+ *   pos:        (n_atoms, 3) doubles, already rescaled and wrapped.
+ *   type_index: (n_atoms) int32 into the type table.
+ *   type_tab:   (n_types, 5) doubles: c1 = Nel/sigma^3, c2 = 2*sigma^2,
+ *               Ax, Ay, Az (the int() of the get_borders widths,
+ *               dens.py:38-43, 287; c1, c2 as dens.py:308 computes them).
+ *   geom:       16 doubles: dr[3], ucell[9] (row major), nborder, 0, 0, 0.
+ */
+int msf_gauss_grid_f64(const msf_plan* plan, const double* pos, const int32_t* type_index,
+                       int64_t n_atoms, const double* type_tab, int32_t n_types,
+                       const double* geom_host, double* grid, msf_stream_t stream);
+/* sf += |rfftn(grid)|^2 for FP64 grids (n_grids of them); the grid is
+ * rounded to FP32 on load and transformed by the same FP32 FFT. */
+int msf_power_accum_f64(msf_plan* plan, const double* grids, int32_t n_grids, double* sf,
+                        msf_stream_t stream);
+
+/* ------------------------------------------------------ plot array (a10)
+ * sfplt = get_dplot(sf) (dens.py:142-163): fftshift in x and y, Hermitian
+ * mirror in z, z-Nyquist dropped, DC := mean of its +x/+y/+z neighbours,
+ * one voxel trimmed per face.  sf (n0, n1, nh) -> out (n0-2, n1-2, 2nh-3).
+ */
+int msf_sfplt(const double* sf, int32_t n0, int32_t n1, int32_t nh, double* out,
+              msf_stream_t stream);
+
+/* ---------------------------------------------------- Ewald slices (a12)
+ * plot2d.Plot_Ewald_Sphere_Correction (plot2d.py:218-267): trilinear
+ * interpolation (NaN outside) of the centred array D (p0, p1, p2) with axis
+ * coordinates X, Y, Z at the Ewald-sphere points of the xy, xz and yz
+ * planes, K = 2 pi / lambda.  Outputs (p0,p1), (p0,p2), (p1,p2).
+ */
+int msf_ewald(const double* D, int32_t p0, int32_t p1, int32_t p2, const double* X,
+              const double* Y, const double* Z, double K, double* xy, double* xz, double* yz,
+              msf_stream_t stream);
+
+/* ----------------------------------------------------- direct sum (a13)
+ * S_q = |sum_j f_j exp(i q.r_j)|^2 for n_sys systems of n_atoms atoms and
+ * n_q vectors each (FP32).  r_f: (n_sys, n_atoms) float4 (x, y, z, f);
+ * q: (n_sys, n_q) float4 (qx, qy, qz, unused), or (n_q) shared by every
+ * system when q_shared != 0; S: (n_sys, n_q) float; AB: (n_sys, n_q) float2
+ * (A = sum f cos, B = sum f sin), saved for the adjoint.  No reference
+ * counterpart: the continuous-position form of dens.py:313-316.
+ */
+int msf_direct_fwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q, int32_t n_sys,
+                   int32_t q_shared, float* S, void* AB, msf_stream_t stream);
+/* Adjoint: given g = dL/dS (n_sys, n_q) float, writes (n_sys, n_atoms)
+ * float4 (dL/dx, dL/dy, dL/dz, dL/df).  Recomputes the phases; no N x M
+ * storage. */
+int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q, int32_t n_sys,
+                   int32_t q_shared, const float* g, const void* AB, void* grad,
+                   msf_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSF_H_ */

@@ -1,0 +1,203 @@
+// msf_direct.cu -- direct-sum structure factor S(q) = |sum_j f_j e^{i q.r_j}|^2
+// and its adjoint, in FP32 (the continuous-position form of the gridded
+// power the reference computes at dens.py:313-316).
+//
+// Phases are computed in turns, t = (q/2pi).r, and reduced to [-1/2, 1/2]
+// before the SFU sin/cos (__sincosf(2 pi t) on [-pi, pi]).  With |q.r| up
+// to ~25 turns a plain FP32 product loses ~1e-5 rad, so each q/2pi is held
+// as an unevaluated sum hi + lo (split from FP64), each product q_i r_i is
+// formed with its exact FMA residual, every component is reduced by its own
+// nearest integer (exact), and the small remainders are summed: the phase
+// error is then a few 1e-7 turn whatever |q.r| is.  Partial sums over one
+// shared-memory tile are FP32 and are added to FP64 running sums per tile.
+//
+// Forward: A_q = sum f cos, B_q = sum f sin, S_q = A^2 + B^2.
+// Adjoint (upstream g_q = dL/dS_q), recomputing the phases:
+//   dL/dr_j = 2 f_j sum_q g_q q (B_q cos - A_q sin)
+//   dL/df_j = 2 sum_q g_q (A_q cos + B_q sin)
+#include "msf_internal.cuh"
+
+namespace msf {
+
+constexpr int kDThreads = 256;
+constexpr int kDPer = 2;                       // q (fwd) or atoms (bwd) per thread
+constexpr int kDTile = 512;                    // atoms (fwd) or q (bwd) per smem tile
+constexpr float k2Pi = 6.28318530717958648f;
+
+// q in turns as hi + lo pairs: (hx, hy, hz) and (lx, ly, lz)
+struct QTurns { float hx, hy, hz, lx, ly, lz; };
+
+__device__ __forceinline__ QTurns q_turns(float4 q) {
+  const double inv = 0.15915494309189533577;  // 1/(2 pi)
+  const double tx = (double)q.x * inv, ty = (double)q.y * inv, tz = (double)q.z * inv;
+  QTurns t;
+  t.hx = (float)tx; t.hy = (float)ty; t.hz = (float)tz;
+  t.lx = (float)(tx - (double)t.hx);
+  t.ly = (float)(ty - (double)t.hy);
+  t.lz = (float)(tz - (double)t.hz);
+  return t;
+}
+
+// fractional turns of (hi + lo) * r, reduced per component
+__device__ __forceinline__ float turn_frac(float hi, float lo, float r) {
+  const float p = hi * r;
+  const float e = fmaf(lo, r, fmaf(hi, r, -p));  // exact residual of hi*r, plus lo*r
+  return (p - rintf(p)) + e;
+}
+
+__device__ __forceinline__ void phase_sincos(const QTurns& q, float4 r, float* s, float* c) {
+  float t = turn_frac(q.hx, q.lx, r.x) + turn_frac(q.hy, q.ly, r.y) + turn_frac(q.hz, q.lz, r.z);
+  t -= rintf(t);
+  __sincosf(k2Pi * t, s, c);
+}
+
+__global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
+                                                          const float4* __restrict__ q, int64_t n_q,
+                                                          int64_t q_sys_stride, float* S, float2* AB) {
+  __shared__ float4 tile[kDTile];
+  const int sys = blockIdx.y;
+  const float4* R = rf + sys * n_atoms;
+  const float4* Q = q + sys * q_sys_stride;
+  QTurns tq[kDPer];
+  int64_t qi[kDPer];
+  double A[kDPer], B[kDPer];
+#pragma unroll
+  for (int k = 0; k < kDPer; ++k) {
+    qi[k] = (int64_t)blockIdx.x * kDThreads * kDPer + k * kDThreads + threadIdx.x;
+    float4 v = qi[k] < n_q ? __ldg(Q + qi[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    tq[k] = q_turns(v);
+    A[k] = 0.0; B[k] = 0.0;
+  }
+  for (int64_t a0 = 0; a0 < n_atoms; a0 += kDTile) {
+    const int na = (int)min((int64_t)kDTile, n_atoms - a0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < na; i += kDThreads) tile[i] = __ldg(R + a0 + i);
+    __syncthreads();
+    float pa[kDPer], pb[kDPer];
+#pragma unroll
+    for (int k = 0; k < kDPer; ++k) { pa[k] = 0.f; pb[k] = 0.f; }
+    for (int i = 0; i < na; ++i) {
+      const float4 r = tile[i];
+#pragma unroll
+      for (int k = 0; k < kDPer; ++k) {
+        float s, c;
+        phase_sincos(tq[k], r, &s, &c);
+        pa[k] = fmaf(r.w, c, pa[k]);
+        pb[k] = fmaf(r.w, s, pb[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kDPer; ++k) { A[k] += (double)pa[k]; B[k] += (double)pb[k]; }
+  }
+#pragma unroll
+  for (int k = 0; k < kDPer; ++k) {
+    if (qi[k] < n_q) {
+      const int64_t o = sys * n_q + qi[k];
+      S[o] = (float)(A[k] * A[k] + B[k] * B[k]);
+      AB[o] = make_float2((float)A[k], (float)B[k]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restrict__ rf, int64_t n_atoms,
+                                                          const float4* __restrict__ q, int64_t n_q,
+                                                          int64_t q_sys_stride, const float* __restrict__ g,
+                                                          const float2* __restrict__ AB, float4* grad) {
+  __shared__ QTurns tq[kDTile];   // q/2pi as hi + lo
+  __shared__ float4 tqr[kDTile];  // q (rad)
+  __shared__ float2 tg[kDTile];   // (g*A, g*B)
+  const int sys = blockIdx.y;
+  const float4* R = rf + sys * n_atoms;
+  const float4* Q = q + sys * q_sys_stride;
+  float4 r[kDPer];
+  int64_t ai[kDPer];
+  double gx[kDPer], gy[kDPer], gz[kDPer], gf[kDPer];
+#pragma unroll
+  for (int k = 0; k < kDPer; ++k) {
+    ai[k] = (int64_t)blockIdx.x * kDThreads * kDPer + k * kDThreads + threadIdx.x;
+    r[k] = ai[k] < n_atoms ? __ldg(R + ai[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    gx[k] = gy[k] = gz[k] = gf[k] = 0.0;
+  }
+  for (int64_t q0 = 0; q0 < n_q; q0 += kDTile) {
+    const int nq = (int)min((int64_t)kDTile, n_q - q0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nq; i += kDThreads) {
+      const float4 v = __ldg(Q + q0 + i);
+      tqr[i] = v;
+      tq[i] = q_turns(v);
+      const float gg = __ldg(g + sys * n_q + q0 + i);
+      const float2 ab = __ldg(AB + sys * n_q + q0 + i);
+      tg[i] = make_float2(gg * ab.x, gg * ab.y);
+    }
+    __syncthreads();
+    float px[kDPer], py[kDPer], pz[kDPer], pf[kDPer];
+#pragma unroll
+    for (int k = 0; k < kDPer; ++k) px[k] = py[k] = pz[k] = pf[k] = 0.f;
+    for (int i = 0; i < nq; ++i) {
+      const QTurns t = tq[i];
+      const float4 qq = tqr[i];
+      const float2 ga = tg[i];
+#pragma unroll
+      for (int k = 0; k < kDPer; ++k) {
+        float s, c;
+        phase_sincos(t, r[k], &s, &c);
+        const float w = fmaf(ga.y, c, -ga.x * s);   // gB cos - gA sin
+        px[k] = fmaf(w, qq.x, px[k]);
+        py[k] = fmaf(w, qq.y, py[k]);
+        pz[k] = fmaf(w, qq.z, pz[k]);
+        pf[k] = fmaf(ga.x, c, fmaf(ga.y, s, pf[k]));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kDPer; ++k) {
+      gx[k] += (double)px[k]; gy[k] += (double)py[k]; gz[k] += (double)pz[k]; gf[k] += (double)pf[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kDPer; ++k) {
+    if (ai[k] < n_atoms) {
+      const double f2 = 2.0 * (double)r[k].w;
+      grad[sys * n_atoms + ai[k]] =
+          make_float4((float)(f2 * gx[k]), (float)(f2 * gy[k]), (float)(f2 * gz[k]), (float)(2.0 * gf[k]));
+    }
+  }
+}
+
+}  // namespace msf
+
+using namespace msf;
+
+extern "C" {
+
+int msf_direct_fwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q, int32_t n_sys,
+                   int32_t q_shared, float* S, void* AB, msf_stream_t stream) {
+  if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
+  if (n_q == 0) return MSF_OK;
+  if (!q || !S || !AB || (n_atoms > 0 && !r_f)) return MSF_E_INVALID;
+  const int64_t per = (int64_t)kDThreads * kDPer;
+  const int64_t nb = (n_q + per - 1) / per;
+  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
+  dim3 grid((unsigned)nb, n_sys);
+  k_direct_fwd<<<grid, kDThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      static_cast<const float4*>(r_f), n_atoms, static_cast<const float4*>(q), n_q,
+      q_shared ? 0 : n_q, S, static_cast<float2*>(AB));
+  return launch_status();
+}
+
+int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q, int32_t n_sys,
+                   int32_t q_shared, const float* g, const void* AB, void* grad,
+                   msf_stream_t stream) {
+  if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
+  if (n_atoms == 0) return MSF_OK;
+  if (!r_f || !grad || (n_q > 0 && (!q || !g || !AB))) return MSF_E_INVALID;
+  const int64_t per = (int64_t)kDThreads * kDPer;
+  const int64_t nb = (n_atoms + per - 1) / per;
+  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
+  dim3 grid((unsigned)nb, n_sys);
+  k_direct_bwd<<<grid, kDThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      static_cast<const float4*>(r_f), n_atoms, static_cast<const float4*>(q), n_q,
+      q_shared ? 0 : n_q, g, static_cast<const float2*>(AB), static_cast<float4*>(grad));
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,280 @@
+// msf_hist.cu -- electron-weighted histogram deposit and the fused chain.
+//
+// The reference splats a Gaussian per atom in a Python loop (dens.py:283-311);
+// the plain method bins each atom's integer electron count into the voxel
+// numpy.histogramdd assigns it to, so the int32 grid is bit-exact against
+// np.histogramdd(pos, bins=(n0,n1,n2), range=[(0,L_i)], weights=w):
+//   edges e[i] = i*(L/n), e[n] = L (numpy.linspace); bin = the largest i
+//   with e[i] <= x; x == e[n] goes to bin n-1; x < 0, x > L, NaN dropped.
+//
+// float32 positions without rescale/wrap are binned in FP32 against two
+// tables derived from the FP64 edges: flo[i] = smallest float >= e[i] and
+// fhi[i] = largest float <= e[i].  For a float x, (double)x >= e[i] iff
+// x >= flo[i] and (double)x <= e[i] iff x <= fhi[i], so the FP32 search
+// gives exactly the FP64 answer without FP64 arithmetic (GB300 issues FP64
+// at a small fraction of the FP32 rate).  Rescaled or wrapped positions and
+// FP64 inputs are binned in FP64 with round-to-nearest intrinsics, so the
+// compiler cannot fuse the rescale and wrap arithmetic (dens.py:58, 211-212)
+// into FMAs that numpy does not do.
+//
+// Deposit: one atom per thread, float4 (x, y, z, w) loads, voxels of a warp
+// matched with __match_any_sync and summed with __reduce_add_sync so that a
+// voxel hit by several lanes takes one atomicAdd.
+#include "msf_internal.cuh"
+
+namespace msf {
+
+struct DepArgs {
+  const void* pos;
+  const int32_t* w;
+  int64_t n_atoms;
+  int64_t frame_stride;  // elements (float4 or double) between frames
+  const double* scale;   // (nframes, 3) or null
+  int flags;
+  int n0, n1, n2;
+  double L0, L1, L2;
+  float inv0, inv1, inv2;
+  const double* e0;
+  const double* e1;
+  const double* e2;
+  const float* flo0;
+  const float* flo1;
+  const float* flo2;
+  const float* fhi0;
+  const float* fhi1;
+  const float* fhi2;
+  int32_t* grids;
+  int64_t V;
+};
+
+__device__ __forceinline__ int bin_f32(float x, int n, float inv, const float* __restrict__ flo,
+                                       const float* __restrict__ fhi) {
+  if (!(x >= __ldg(flo)) || !(x <= __ldg(fhi + n))) return -1;  // also drops NaN
+  int b = (int)(x * inv);
+  b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
+  while (b > 0 && x < __ldg(flo + b)) --b;
+  while (b < n - 1 && x >= __ldg(flo + b + 1)) ++b;
+  return b;
+}
+
+__device__ __forceinline__ int bin_f64(double x, int n, float inv, const double* __restrict__ e) {
+  if (!(x >= __ldg(e)) || !(x <= __ldg(e + n))) return -1;
+  int b = (int)((float)x * inv);
+  b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
+  while (b > 0 && x < __ldg(e + b)) --b;
+  while (b < n - 1 && x >= __ldg(e + b + 1)) ++b;
+  return b;
+}
+
+// dens.py:52-58 (per-frame rescale) and dens.py:211-212 (wrap), in FP64.
+__device__ __forceinline__ double prep(double x, const double* s, int axis, bool wrap, double L) {
+  if (s) x = __dmul_rn(x, __ldg(s + axis));
+  if (wrap) {
+    x = (x < L) ? x : __dsub_rn(x, L);
+    x = (x > 0.0) ? x : __dadd_rn(x, L);
+  }
+  return x;
+}
+
+// MODE 0: float4, FP32 binning; 1: float4, FP64 rescale/wrap; 2: FP64 (N,3) + int32 weights;
+// 3: float (N,3) + int32 weights, FP32 binning; 4: float (N,3) + int32 weights, FP64 rescale/wrap
+template <int MODE>
+__global__ void k_hist_deposit(DepArgs a) {
+  const int frame = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool valid = i < a.n_atoms;
+  int b0 = -1, b1 = -1, b2 = -1, wgt = 0;
+  if (valid) {
+    const double* s = a.scale ? a.scale + 3 * frame : nullptr;
+    const bool wrap = a.flags & MSF_WRAP;
+    if (MODE == 2) {
+      const double* r = static_cast<const double*>(a.pos) + frame * a.frame_stride + 3 * i;
+      wgt = __ldg(a.w + i);
+      b0 = bin_f64(prep(__ldg(r + 0), s, 0, wrap, a.L0), a.n0, a.inv0, a.e0);
+      b1 = bin_f64(prep(__ldg(r + 1), s, 1, wrap, a.L1), a.n1, a.inv1, a.e1);
+      b2 = bin_f64(prep(__ldg(r + 2), s, 2, wrap, a.L2), a.n2, a.inv2, a.e2);
+    } else if (MODE >= 3) {
+      const float* r = static_cast<const float*>(a.pos) + frame * a.frame_stride + 3 * i;
+      wgt = __ldg(a.w + i);
+      const float x = __ldg(r + 0), y = __ldg(r + 1), z = __ldg(r + 2);
+      if (MODE == 3) {
+        b0 = bin_f32(x, a.n0, a.inv0, a.flo0, a.fhi0);
+        b1 = bin_f32(y, a.n1, a.inv1, a.flo1, a.fhi1);
+        b2 = bin_f32(z, a.n2, a.inv2, a.flo2, a.fhi2);
+      } else {
+        b0 = bin_f64(prep((double)x, s, 0, wrap, a.L0), a.n0, a.inv0, a.e0);
+        b1 = bin_f64(prep((double)y, s, 1, wrap, a.L1), a.n1, a.inv1, a.e1);
+        b2 = bin_f64(prep((double)z, s, 2, wrap, a.L2), a.n2, a.inv2, a.e2);
+      }
+    } else {
+      const float4 v = __ldg(static_cast<const float4*>(a.pos) + frame * a.frame_stride + i);
+      wgt = __float2int_rn(v.w);
+      if (MODE == 0) {
+        b0 = bin_f32(v.x, a.n0, a.inv0, a.flo0, a.fhi0);
+        b1 = bin_f32(v.y, a.n1, a.inv1, a.flo1, a.fhi1);
+        b2 = bin_f32(v.z, a.n2, a.inv2, a.flo2, a.fhi2);
+      } else {
+        b0 = bin_f64(prep((double)v.x, s, 0, wrap, a.L0), a.n0, a.inv0, a.e0);
+        b1 = bin_f64(prep((double)v.y, s, 1, wrap, a.L1), a.n1, a.inv1, a.e1);
+        b2 = bin_f64(prep((double)v.z, s, 2, wrap, a.L2), a.n2, a.inv2, a.e2);
+      }
+    }
+    valid = (b0 >= 0) & (b1 >= 0) & (b2 >= 0);
+  }
+  const unsigned vm = __ballot_sync(0xffffffffu, valid);
+  if (valid) {
+    const int64_t key = frame * a.V + ((int64_t)b0 * a.n1 + b1) * a.n2 + b2;
+    const unsigned peers = __match_any_sync(vm, (unsigned long long)key);
+    const int sum = __reduce_add_sync(peers, wgt);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(a.grids + key, sum);
+  }
+}
+
+static DepArgs dep_args(const msf_plan* p) {
+  DepArgs a;
+  a.n0 = p->n0; a.n1 = p->n1; a.n2 = p->n2;
+  a.L0 = p->box[0]; a.L1 = p->box[1]; a.L2 = p->box[2];
+  a.inv0 = (float)(p->n0 / p->box[0]);
+  a.inv1 = (float)(p->n1 / p->box[1]);
+  a.inv2 = (float)(p->n2 / p->box[2]);
+  const double* e = ws_ptr<double>(p, p->off_edges_d);
+  const float* lo = ws_ptr<float>(p, p->off_edges_flo);
+  const float* hi = ws_ptr<float>(p, p->off_edges_fhi);
+  const int o1 = p->n0 + 1, o2 = p->n0 + p->n1 + 2;
+  a.e0 = e; a.e1 = e + o1; a.e2 = e + o2;
+  a.flo0 = lo; a.flo1 = lo + o1; a.flo2 = lo + o2;
+  a.fhi0 = hi; a.fhi1 = hi + o1; a.fhi2 = hi + o2;
+  a.V = grid_elems(p);
+  return a;
+}
+
+int hist_deposit_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
+                       int64_t n_atoms, int nframes, int64_t frame_stride, const double* scale,
+                       int flags, int32_t* grids, cudaStream_t st) {
+  if (n_atoms <= 0 || nframes <= 0) return MSF_OK;
+  DepArgs a = dep_args(p);
+  a.pos = pos;
+  a.w = weights;
+  a.n_atoms = n_atoms;
+  a.frame_stride = frame_stride;
+  a.scale = scale;
+  a.flags = flags;
+  a.grids = grids;
+  const int bs = p->deposit_block;
+  const int64_t nb = (n_atoms + bs - 1) / bs;
+  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
+  dim3 grid((unsigned)nb, nframes);
+  const bool fp64_prep = scale || (flags & MSF_WRAP);
+  if (layout == kLayoutF64) k_hist_deposit<2><<<grid, bs, 0, st>>>(a);
+  else if (layout == kLayoutF32xyz) {
+    if (fp64_prep) k_hist_deposit<4><<<grid, bs, 0, st>>>(a);
+    else k_hist_deposit<3><<<grid, bs, 0, st>>>(a);
+  } else {
+    if (fp64_prep) k_hist_deposit<1><<<grid, bs, 0, st>>>(a);
+    else k_hist_deposit<0><<<grid, bs, 0, st>>>(a);
+  }
+  return launch_status();
+}
+
+}  // namespace msf
+
+using namespace msf;
+
+static int check_flags(int flags) { return (flags & ~MSF_WRAP) ? MSF_E_INVALID : MSF_OK; }
+
+extern "C" {
+
+int msf_hist_grid_f32(const msf_plan* p, const void* pos_w, int64_t n_atoms, const double* scale,
+                      int32_t flags, int32_t* grid, msf_stream_t stream) {
+  if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && !pos_w)) return MSF_E_INVALID;
+  if (!p->bound) return MSF_E_NOT_BOUND;
+  if (check_flags(flags)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos_w, nullptr, kLayoutF32x4, n_atoms, 1, n_atoms, scale, flags,
+                            grid, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int msf_hist_grid_f32xyz(const msf_plan* p, const float* pos, const int32_t* weights,
+                         int64_t n_atoms, const double* scale, int32_t flags, int32_t* grid,
+                         msf_stream_t stream) {
+  if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && (!pos || !weights))) return MSF_E_INVALID;
+  if (!p->bound) return MSF_E_NOT_BOUND;
+  if (check_flags(flags)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos, weights, kLayoutF32xyz, n_atoms, 1, 3 * n_atoms, scale, flags,
+                            grid, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int msf_hist_grid_f64(const msf_plan* p, const double* pos, const int32_t* weights,
+                      int64_t n_atoms, const double* scale, int32_t flags, int32_t* grid,
+                      msf_stream_t stream) {
+  if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && (!pos || !weights))) return MSF_E_INVALID;
+  if (!p->bound) return MSF_E_NOT_BOUND;
+  if (check_flags(flags)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos, weights, kLayoutF64, n_atoms, 1, 3 * n_atoms, scale, flags,
+                            grid, reinterpret_cast<cudaStream_t>(stream));
+}
+
+static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int layout,
+                       int64_t n_atoms, int64_t n_frames, const double* scale, int32_t flags,
+                       double* sf, msf_stream_t stream) {
+  if (!p || !sf || n_atoms < 0 || n_frames < 0) return MSF_E_INVALID;
+  if (n_atoms > 0 && n_frames > 0 && (!pos || (layout != kLayoutF32x4 && !weights)))
+    return MSF_E_INVALID;
+  if (!p->bound) return MSF_E_NOT_BOUND;
+  if (check_flags(flags)) return MSF_E_INVALID;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
+  const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
+  const size_t esize = layout == kLayoutF32x4 ? 4 * sizeof(float)
+                       : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
+  for (int64_t f = 0; f < n_frames; f += p->batch) {
+    const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
+    const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;
+    int s = hist_deposit_batch(p, fp, weights, layout, n_atoms, nb, fstride,
+                               scale ? scale + 3 * f : nullptr, flags, grids, st);
+    if (s) return s;
+    s = fft_power_batch(p, grids, kGridI32, nb, sf, 1, st);
+    if (s) return s;
+  }
+  return MSF_OK;
+}
+
+int msf_hist_sf_f32(msf_plan* p, const void* pos_w, int64_t n_atoms, int64_t n_frames,
+                    const double* scale, int32_t flags, double* sf, msf_stream_t stream) {
+  return hist_sf_any(p, pos_w, nullptr, kLayoutF32x4, n_atoms, n_frames, scale, flags, sf, stream);
+}
+
+int msf_hist_sf_f32xyz(msf_plan* p, const float* pos, const int32_t* weights, int64_t n_atoms,
+                       int64_t n_frames, const double* scale, int32_t flags, double* sf,
+                       msf_stream_t stream) {
+  return hist_sf_any(p, pos, weights, kLayoutF32xyz, n_atoms, n_frames, scale, flags, sf, stream);
+}
+
+int msf_hist_batch_stages(msf_plan* p, int32_t stages, int32_t layout, const void* pos,
+                          const int32_t* weights, int64_t n_atoms, int32_t n_frames,
+                          const double* scale, int32_t flags, double* sf, msf_stream_t stream) {
+  if (!p || n_atoms < 0 || n_frames < 1 || n_frames > p->batch) return MSF_E_INVALID;
+  if (layout < kLayoutF32x4 || layout > kLayoutF32xyz || (stages & ~7) || check_flags(flags))
+    return MSF_E_INVALID;
+  if ((stages & 1) && n_atoms > 0 && (!pos || (layout != kLayoutF32x4 && !weights)))
+    return MSF_E_INVALID;
+  if ((stages & 4) && !sf) return MSF_E_INVALID;
+  if (!p->bound) return MSF_E_NOT_BOUND;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
+  int s = MSF_OK;
+  if (stages & 1) {
+    const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
+    s = hist_deposit_batch(p, pos, weights, layout, n_atoms, n_frames, fstride, scale, flags, grids, st);
+  }
+  if (!s && (stages & 2)) s = fft_stage_a(p, grids, kGridI32, n_frames, 1, st);
+  if (!s && (stages & 4)) s = fft_stage_b(p, n_frames, sf, st);
+  return s;
+}
+
+int msf_hist_sf_f64(msf_plan* p, const double* pos, const int32_t* weights, int64_t n_atoms,
+                    int64_t n_frames, const double* scale, int32_t flags, double* sf,
+                    msf_stream_t stream) {
+  return hist_sf_any(p, pos, weights, kLayoutF64, n_atoms, n_frames, scale, flags, sf, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// msf_post.cu -- centred plot array (get_dplot) and Ewald-sphere slices.
+#include "msf_internal.cuh"
+
+namespace msf {
+
+// dens.py:142-163.  With dmag = sf (n0, n1, nh) and the trimmed output
+// (n0-2, n1-2, 2nh-3) indexed (i, j, k):
+//   k >= nh-2 : sf[(i+1+n0/2) % n0, (j+1+n1/2) % n1, k-nh+2]        (shifted copy)
+//   k <  nh-2 : sf[(n0-1-i+n0/2) % n0, (n1-1-j+n1/2) % n1, nh-2-k]   (z mirror)
+// and the DC voxel (n0/2-1, n1/2-1, nh-2) := 1/3*((sf[1,0,0] + sf[0,1,0]) + sf[0,0,1]).
+__global__ void k_sfplt(const double* __restrict__ sf, int n0, int n1, int nh,
+                        double* __restrict__ out) {
+  const int m0 = n0 - 2, m1 = n1 - 2, m2 = 2 * nh - 3;
+  const int64_t total = (int64_t)m0 * m1 * m2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e % m2);
+    const int64_t r = e / m2;
+    const int j = (int)(r % m1);
+    const int i = (int)(r / m1);
+    int sx, sy, sz;
+    if (k >= nh - 2) {
+      sx = (i + 1 + n0 / 2) % n0;
+      sy = (j + 1 + n1 / 2) % n1;
+      sz = k - nh + 2;
+    } else {
+      sx = (n0 - 1 - i + n0 / 2) % n0;
+      sy = (n1 - 1 - j + n1 / 2) % n1;
+      sz = nh - 2 - k;
+    }
+    double v;
+    if (i == n0 / 2 - 1 && j == n1 / 2 - 1 && k == nh - 2) {
+      const double a = __ldg(sf + (int64_t)1 * n1 * nh);
+      const double b = __ldg(sf + nh);
+      const double c = __ldg(sf + 1);
+      v = __dmul_rn(1.0 / 3.0, __dadd_rn(__dadd_rn(a, b), c));
+    } else {
+      v = __ldg(sf + ((int64_t)sx * n1 + sy) * nh + sz);
+    }
+    out[e] = v;
+  }
+}
+
+// scipy's find_interval_ascending: i with x[i] <= v < x[i+1], the last
+// interval closed on the right; -1 outside [x[0], x[n-1]] or NaN.
+__device__ __forceinline__ int find_interval(const double* __restrict__ x, int n, double v) {
+  const double a = __ldg(x), b = __ldg(x + n - 1);
+  if (!(a <= v && v <= b)) return -1;
+  if (v == b) return n - 2;
+  const double h = __ddiv_rn(__dsub_rn(b, a), (double)(n - 1));
+  int i = (int)((v - a) / h);
+  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  while (i > 0 && v < __ldg(x + i)) --i;
+  while (i < n - 2 && v >= __ldg(x + i + 1)) ++i;
+  return i;
+}
+
+// RegularGridInterpolator(method='linear', bounds_error=False) at one point:
+// corners in itertools.product order (lower before upper, x slowest), weight
+// ((1*w0)*w1)*w2, terms summed in that order; NaN outside the grid.
+__device__ double interp3(const double* __restrict__ D, int p0, int p1, int p2,
+                          const double* X, const double* Y, const double* Z, double x, double y,
+                          double z) {
+  const int i0 = find_interval(X, p0, x);
+  const int i1 = find_interval(Y, p1, y);
+  const int i2 = find_interval(Z, p2, z);
+  if (i0 < 0 || i1 < 0 || i2 < 0) return __longlong_as_double(0x7ff8000000000000LL);
+  const double y0 = __ddiv_rn(__dsub_rn(x, __ldg(X + i0)), __dsub_rn(__ldg(X + i0 + 1), __ldg(X + i0)));
+  const double y1 = __ddiv_rn(__dsub_rn(y, __ldg(Y + i1)), __dsub_rn(__ldg(Y + i1 + 1), __ldg(Y + i1)));
+  const double y2 = __ddiv_rn(__dsub_rn(z, __ldg(Z + i2)), __dsub_rn(__ldg(Z + i2 + 1), __ldg(Z + i2)));
+  const double w[3][2] = {{__dsub_rn(1.0, y0), y0}, {__dsub_rn(1.0, y1), y1}, {__dsub_rn(1.0, y2), y2}};
+  double acc = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int a = (c >> 2) & 1, b = (c >> 1) & 1, d = c & 1;
+    const double wt = __dmul_rn(__dmul_rn(__dmul_rn(1.0, w[0][a]), w[1][b]), w[2][d]);
+    const double v = __ldg(D + ((int64_t)(i0 + a) * p1 + (i1 + b)) * p2 + (i2 + d));
+    acc = __dadd_rn(acc, __dmul_rn(v, wt));
+  }
+  return acc;
+}
+
+// plot2d.py:236-263: theta = atan(sqrt(a^2 + b^2)/K); in-plane coordinates
+// times cos(theta), the third K*(1 - cos(theta)).
+__global__ void k_ewald(const double* __restrict__ D, int p0, int p1, int p2,
+                        const double* __restrict__ X, const double* __restrict__ Y,
+                        const double* __restrict__ Z, double K, double* xy, double* xz,
+                        double* yz) {
+  const int64_t nxy = (int64_t)p0 * p1, nxz = (int64_t)p0 * p2, nyz = (int64_t)p1 * p2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nxy + nxz + nyz;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int plane;
+    int64_t r;
+    if (e < nxy) { plane = 0; r = e; }
+    else if (e < nxy + nxz) { plane = 1; r = e - nxy; }
+    else { plane = 2; r = e - nxy - nxz; }
+    const int nb = plane == 0 ? p1 : p2;
+    const int ia = (int)(r / nb), ib = (int)(r % nb);
+    const double A = plane == 2 ? __ldg(Y + ia) : __ldg(X + ia);
+    const double Bv = plane == 0 ? __ldg(Y + ib) : __ldg(Z + ib);
+    const double rho = sqrt(__dadd_rn(__dmul_rn(A, A), __dmul_rn(Bv, Bv)));
+    const double c = cos(atan(__ddiv_rn(rho, K)));
+    const double ua = __dmul_rn(A, c), ub = __dmul_rn(Bv, c), h = __dmul_rn(K, __dsub_rn(1.0, c));
+    double v;
+    if (plane == 0) { v = interp3(D, p0, p1, p2, X, Y, Z, ua, ub, h); xy[r] = v; }
+    else if (plane == 1) { v = interp3(D, p0, p1, p2, X, Y, Z, ua, h, ub); xz[r] = v; }
+    else { v = interp3(D, p0, p1, p2, X, Y, Z, h, ua, ub); yz[r] = v; }
+  }
+}
+
+}  // namespace msf
+
+using namespace msf;
+
+extern "C" {
+
+int msf_sfplt(const double* sf, int32_t n0, int32_t n1, int32_t nh, double* out,
+              msf_stream_t stream) {
+  if (!sf || !out) return MSF_E_INVALID;
+  if (n0 < 4 || n1 < 4 || nh < 3 || (n0 & 1) || (n1 & 1)) return MSF_E_UNSUPPORTED;
+  const int64_t total = (int64_t)(n0 - 2) * (n1 - 2) * (2 * nh - 3);
+  const int blocks = (int)((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
+  k_sfplt<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(sf, n0, n1, nh, out);
+  return launch_status();
+}
+
+int msf_ewald(const double* D, int32_t p0, int32_t p1, int32_t p2, const double* X,
+              const double* Y, const double* Z, double K, double* xy, double* xz, double* yz,
+              msf_stream_t stream) {
+  if (!D || !X || !Y || !Z || !xy || !xz || !yz) return MSF_E_INVALID;
+  if (p0 < 2 || p1 < 2 || p2 < 2 || !(K > 0.0)) return MSF_E_INVALID;
+  const int64_t total = (int64_t)p0 * p1 + (int64_t)p0 * p2 + (int64_t)p1 * p2;
+  const int blocks = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
+  k_ewald<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(D, p0, p1, p2, X, Y, Z, K,
+                                                                       xy, xz, yz);
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,309 @@
+"""Device API of the structure-factor path (torch tensors in, torch tensors out).
+
+Every function here launches libmsf kernels on the current CUDA stream; there
+is no CPU implementation behind any of them.
+
+* :func:`structure_factor` -- frames -> electron-weighted histogram -> rfftn
+  -> |F|^2 -> FP64 sum over frames (the per-frame loop of dens.py:277-318 in
+  histogram form, rescale dens.py:46-62 and wrap dens.py:204-221 fused).
+* :func:`hist_grid`, :func:`power_accum` -- the two halves separately.
+* :func:`get_dplot` -- dens.py:142-163 on the device.
+* :func:`ewald_slices` -- plot2d.py:218-267 on the device.
+* :class:`DirectSF` -- differentiable direct-sum S(q).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from ._lib import MSF_WRAP, c_p, call
+from .plan import get_plan, stream_ptr
+
+
+def _dev(device):
+    if device is None:
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device(device)
+
+
+def to_device(x, device, dtype=None):
+    """Tensor on `device` (host numpy arrays go through pinned memory)."""
+    if isinstance(x, torch.Tensor):
+        t = x
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(x))
+    if dtype is not None and t.dtype != dtype:
+        t = t.to(dtype)
+    if t.device != device:
+        if t.device.type == "cpu" and not t.is_pinned():
+            t = t.pin_memory()
+        t = t.to(device, non_blocking=True)
+    return t.contiguous()
+
+
+def frame_scale(box):
+    """(scale (T,3) or None, binning box (3,)) as dens.py:52-53 computes them."""
+    b = np.asarray(box.detach().cpu().numpy() if isinstance(box, torch.Tensor) else box,
+                   dtype=np.float64)
+    if b.ndim == 1:
+        return None, b
+    avg = np.average(b, axis=0)
+    return avg / b, avg
+
+
+def _ptr(t):
+    return c_p(t.data_ptr()) if t is not None else c_p(0)
+
+
+_side_streams = {}
+
+
+def _side_stream(device):
+    s = _side_streams.get(device)
+    if s is None:
+        s = torch.cuda.Stream(device)
+        _side_streams[device] = s
+    return s
+
+
+_CHAIN = {4: "msf_hist_sf_f32", 3: "msf_hist_sf_f32xyz", 8: "msf_hist_sf_f64"}
+
+
+def _launch_chain(plan, code, p, w, N, T, sc, flags, sf, st):
+    if code == 4:
+        call("msf_hist_sf_f32", plan.handle, c_p(p), N, T, c_p(sc), flags, _ptr(sf), st)
+    else:
+        call(_CHAIN[code], plan.handle, c_p(p), c_p(w), N, T, c_p(sc), flags, _ptr(sf), st)
+
+
+def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False, mean=False,
+                     out=None, device=None, tuning=None, stream_chunk=None):
+    """Sum over frames of |rfftn(histogram)|^2, FP64, shape (n0, n1, n2//2+1).
+
+    positions: (T, N, 3) or (N, 3) float32/float64, or (T, N, 4) float32 with
+      the electron count in the 4th component (then ``weights`` is ignored).
+      Host arrays are streamed to the device in chunks of ``stream_chunk``
+      frames on a side stream (double-buffered, pinned memory), overlapping
+      the copies with the kernels of the previous chunk.
+    box: (3,) box edges, or (T, 3) per-frame boxes (frames are rescaled to
+      the mean box as dens.py:46-62 does and binned in the mean box).
+    weights: (N,) integer electron counts.
+    grid_dims: (n0, n1, n2).
+    wrap: apply the reference's periodic wrap before binning (dens.py:211-212);
+      otherwise atoms outside [0, L] are dropped (numpy.histogramdd range).
+    mean: divide by the frame count (the reference saves the undivided sum).
+    out: FP64 tensor to accumulate into (not zeroed).
+    """
+    device = _dev(device)
+    pos = positions
+    if pos.ndim == 2:
+        pos = pos[None]
+    T, N, C = pos.shape
+    scale, L = frame_scale(box)
+    plan = get_plan(grid_dims, L, device=device, **(tuning or {}))
+    if out is None:
+        sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=device)
+    else:
+        sf = out
+        if tuple(sf.shape) != plan.half_shape or sf.dtype != torch.float64 or not sf.is_contiguous():
+            raise ValueError("out must be a contiguous float64 tensor of shape %s" % (plan.half_shape,))
+    flags = MSF_WRAP if wrap else 0
+    is64 = (pos.dtype == torch.float64) if isinstance(pos, torch.Tensor) else (pos.dtype == np.float64)
+    if C == 4:
+        code, tdt, esz = 4, torch.float32, 16
+    elif C == 3:
+        if weights is None:
+            raise ValueError("weights are required for (T, N, 3) positions")
+        code, tdt, esz = (8, torch.float64, 24) if is64 else (3, torch.float32, 12)
+    else:
+        raise ValueError("positions must be (T, N, 3) or (T, N, 4)")
+    host = not (isinstance(pos, torch.Tensor) and pos.device.type == "cuda")
+    with torch.cuda.device(device):
+        st = stream_ptr(device)
+        sc = None if scale is None else to_device(scale, device, torch.float64)
+        wd = None
+        if code != 4:
+            wd = to_device(weights, device, torch.int32)
+            if wd.numel() != N:
+                raise ValueError("weights must have one entry per atom")
+        wptr = wd.data_ptr() if wd is not None else 0
+        scp = sc.data_ptr() if sc is not None else 0
+        chunk = int(stream_chunk or 4 * plan.batch)
+        if not host or T <= chunk or N == 0:
+            p = to_device(pos, device, tdt)
+            _launch_chain(plan, code, p.data_ptr(), wptr, N, T, scp, flags, sf, st)
+        else:
+            hp = pos if isinstance(pos, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(pos))
+            if hp.dtype != tdt:
+                hp = hp.to(tdt)
+            if not hp.is_pinned():
+                hp = hp.contiguous().pin_memory()
+            main = torch.cuda.current_stream(device)
+            side = _side_stream(device)
+            bufs = [torch.empty((chunk, N, C), dtype=tdt, device=device) for _ in range(2)]
+            copied = [torch.cuda.Event() for _ in range(2)]
+            free = [None, None]
+            for b in bufs:
+                b.record_stream(side)
+            for i, f0 in enumerate(range(0, T, chunk)):
+                k = min(chunk, T - f0)
+                b = i % 2
+                with torch.cuda.stream(side):
+                    if free[b] is not None:
+                        side.wait_event(free[b])
+                    bufs[b][:k].copy_(hp[f0:f0 + k], non_blocking=True)
+                    copied[b].record(side)
+                main.wait_event(copied[b])
+                _launch_chain(plan, code, bufs[b].data_ptr(), wptr, N, k,
+                              scp + 24 * f0 if scp else 0, flags, sf, st)
+                ev = torch.cuda.Event()
+                ev.record(main)
+                free[b] = ev
+    if mean and T > 0:
+        sf.div_(T)
+    return sf
+
+
+def hist_grid(positions, box, weights=None, grid_dims=None, *, scale=None, wrap=False, device=None,
+              out=None):
+    """int32 density grid of one frame (bit-exact numpy.histogramdd)."""
+    device = _dev(device)
+    plan = get_plan(grid_dims, np.asarray(box, np.float64), device=device)
+    g = out if out is not None else torch.zeros(tuple(plan.dims), dtype=torch.int32, device=device)
+    N = positions.shape[0]
+    flags = MSF_WRAP if wrap else 0
+    with torch.cuda.device(device):
+        st = stream_ptr(device)
+        sc = None if scale is None else to_device(np.asarray(scale, np.float64), device, torch.float64)
+        if positions.shape[-1] == 4:
+            p = to_device(positions, device, torch.float32)
+            call("msf_hist_grid_f32", plan.handle, _ptr(p), N, _ptr(sc), flags, _ptr(g), st)
+        else:
+            w = to_device(weights, device, torch.int32)
+            is64 = (positions.dtype == torch.float64) if isinstance(positions, torch.Tensor) \
+                else (positions.dtype == np.float64)
+            if is64:
+                p = to_device(positions, device, torch.float64)
+                call("msf_hist_grid_f64", plan.handle, _ptr(p), _ptr(w), N, _ptr(sc), flags, _ptr(g), st)
+            else:
+                p = to_device(positions, device, torch.float32)
+                call("msf_hist_grid_f32xyz", plan.handle, _ptr(p), _ptr(w), N, _ptr(sc), flags,
+                     _ptr(g), st)
+    return g
+
+
+def power_accum(grids, sf=None, *, device=None, tuning=None):
+    """sf += sum_g |rfftn(g)|^2 for grids (G, n0, n1, n2) int32 / float32 / float64."""
+    device = _dev(device)
+    g = to_device(grids, device)
+    if g.ndim == 3:
+        g = g[None]
+    dims = tuple(g.shape[1:])
+    plan = get_plan(dims, (1.0, 1.0, 1.0), device=device, **(tuning or {}))
+    if sf is None:
+        sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=device)
+    fn = {torch.int32: "msf_power_accum_i32", torch.float32: "msf_power_accum_f32",
+          torch.float64: "msf_power_accum_f64"}[g.dtype]
+    with torch.cuda.device(device):
+        call(fn, plan.handle, _ptr(g), g.shape[0], _ptr(sf), stream_ptr(device))
+    return sf
+
+
+def get_dplot(sf):
+    """dens.py:142-163 on the device: (n0, n1, nh) -> (n0-2, n1-2, 2nh-3)."""
+    n0, n1, nh = sf.shape
+    out = torch.empty((n0 - 2, n1 - 2, 2 * nh - 3), dtype=torch.float64, device=sf.device)
+    with torch.cuda.device(sf.device):
+        call("msf_sfplt", _ptr(sf), n0, n1, nh, _ptr(out), stream_ptr(sf.device))
+    return out
+
+
+def plot_axes(half_shape, L):
+    """kgridplt axis coordinates, dens.py:336-342: (ix - n/2)*2*pi/L with true division."""
+    n = (half_shape[0] - 2, half_shape[1] - 2, half_shape[2] * 2 - 3)
+    return [np.array([(ix - n[a] / 2) * 2.0 * math.pi / L[a] for ix in range(n[a])]) for a in range(3)]
+
+
+def ewald_slices(D, X, Y, Z, wavelength):
+    """Ewald-sphere slices (xy, xz, yz) of D (p0, p1, p2) with axes X, Y, Z."""
+    dev = D.device
+    X = to_device(np.asarray(X, np.float64), dev)
+    Y = to_device(np.asarray(Y, np.float64), dev)
+    Z = to_device(np.asarray(Z, np.float64), dev)
+    p0, p1, p2 = D.shape
+    xy = torch.empty((p0, p1), dtype=torch.float64, device=dev)
+    xz = torch.empty((p0, p2), dtype=torch.float64, device=dev)
+    yz = torch.empty((p1, p2), dtype=torch.float64, device=dev)
+    K = 2.0 * math.pi / float(wavelength)
+    with torch.cuda.device(dev):
+        call("msf_ewald", _ptr(D.contiguous()), p0, p1, p2, _ptr(X), _ptr(Y), _ptr(Z), K,
+             _ptr(xy), _ptr(xz), _ptr(yz), stream_ptr(dev))
+    return xy, xz, yz
+
+
+def ewald_from_sf(sf, L, wavelength):
+    """get_dplot + kgridplt axes + Ewald slices, all on the device."""
+    D = get_dplot(sf)
+    X, Y, Z = plot_axes(tuple(sf.shape), L)
+    return ewald_slices(D, X, Y, Z, wavelength)
+
+
+# ------------------------------------------------------------ direct sum
+def _pack_rf(r, f):
+    if f.dim() == r.dim() - 1:
+        return torch.cat([r, f.unsqueeze(-1)], dim=-1).contiguous()
+    raise ValueError("f must have one weight per atom")
+
+
+class DirectSF(torch.autograd.Function):
+    """S(q) = |sum_j f_j exp(i q.r_j)|^2 with a hand-written adjoint.
+
+    r: (N, 3) or (S, N, 3) float32 CUDA; f: (N,) or (S, N); q: (M, 3) shared
+    or (S, M, 3).  Returns (M,) or (S, M).  Gradients flow to r and f.
+    """
+
+    @staticmethod
+    def forward(ctx, r, f, q):
+        squeeze = r.dim() == 2
+        r3 = r.unsqueeze(0) if squeeze else r
+        f2 = f.unsqueeze(0) if f.dim() == 1 and not squeeze else (f.unsqueeze(0) if squeeze else f)
+        if f2.shape[0] != r3.shape[0]:
+            f2 = f2.expand(r3.shape[0], -1)
+        S_, N = r3.shape[0], r3.shape[1]
+        rf = _pack_rf(r3.float(), f2.float())
+        q_shared = q.dim() == 2
+        M = q.shape[-2]
+        q4 = torch.cat([q.float(), torch.zeros(q.shape[:-1] + (1,), device=q.device)], -1).contiguous()
+        Sq = torch.empty((S_, M), dtype=torch.float32, device=r.device)
+        AB = torch.empty((S_, M, 2), dtype=torch.float32, device=r.device)
+        with torch.cuda.device(r.device):
+            call("msf_direct_fwd", _ptr(rf), N, _ptr(q4), M, S_, int(q_shared), _ptr(Sq), _ptr(AB),
+                 stream_ptr(r.device))
+        ctx.save_for_backward(rf, q4, AB)
+        ctx.meta = (squeeze, q_shared, f.dim())
+        return Sq[0] if squeeze else Sq
+
+    @staticmethod
+    def backward(ctx, gS):
+        rf, q4, AB = ctx.saved_tensors
+        squeeze, q_shared, fdim = ctx.meta
+        S_, N = rf.shape[0], rf.shape[1]
+        M = q4.shape[-2]
+        g = (gS.unsqueeze(0) if squeeze else gS).float().contiguous()
+        grad = torch.empty((S_, N, 4), dtype=torch.float32, device=rf.device)
+        with torch.cuda.device(rf.device):
+            call("msf_direct_bwd", _ptr(rf), N, _ptr(q4), M, S_, int(q_shared), _ptr(g), _ptr(AB),
+                 _ptr(grad), stream_ptr(rf.device))
+        gr = grad[..., :3]
+        gf = grad[..., 3]
+        if squeeze:
+            gr, gf = gr[0], gf[0]
+        elif fdim == 1:
+            gf = gf.sum(0)
+        return gr, gf, None
+
+
+def direct_sf(r, f, q):
+    return DirectSF.apply(r, f, q)

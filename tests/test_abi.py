@@ -1,0 +1,104 @@
+"""The C ABI library without a GPU: it loads, exports every symbol that
+include/msf.h declares, and its host-side argument checks return the
+documented status codes (no kernel is launched by any call here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+import mdsf
+from mdsf import _lib
+
+HEADER = os.path.join(ROOT, "include", "msf.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(msf_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = mdsf.load()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
+
+
+def test_strerror_and_version():
+    lib = mdsf.load()
+    assert lib.msf_version() >= 100
+    for code in _lib.ERRORS:
+        assert lib.msf_strerror(code)
+    assert lib.msf_strerror(-5) == b"atom outside the padded grid"
+
+
+def _desc(dims=(64, 64, 64), box=(2.5, 2.5, 2.5), **kw):
+    d = _lib.PlanDesc(*dims, kw.get("batch", 0), (C.c_double * 3)(*box), kw.get("variant", 0),
+                      kw.get("tile_w", 0), kw.get("rows_per_block", 0), kw.get("deposit_block", 0))
+    return d
+
+
+def create(**kw):
+    lib = mdsf.load()
+    h = C.c_void_p()
+    st = lib.msf_plan_create(C.byref(h), C.byref(_desc(**kw)))
+    return st, h
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(dims=(1, 64, 64)), -2), (dict(dims=(64, 2048, 64)), -2), (dict(box=(0.0, 1, 1)), -1),
+    (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=3), -1),
+    (dict(tile_w=12), -1), (dict(deposit_block=100), -1),
+])
+def test_plan_create_rejects(kw, code):
+    st, h = create(**kw)
+    assert st == code
+
+
+def test_plan_layout_and_query():
+    lib = mdsf.load()
+    st, h = create(dims=(256, 256, 128), box=(16.0, 13.856, 8.0), batch=4)
+    assert st == 0
+    ws = lib.msf_plan_workspace_bytes(h)
+    V, Vh = 256 * 256 * 128, 256 * 256 * 65
+    assert ws >= 4 * (4 * V + 8 * Vh)
+    q = (C.c_int32 * 8)()
+    assert lib.msf_plan_query(h, q) == 0
+    assert q[0] == 1 and q[3] == 4 and q[7] == 65   # fused plane variant, batch 4, nh
+    # an unbound plan refuses work before touching the GPU
+    assert lib.msf_hist_sf_f32(h, C.c_void_p(16), 10, 1, None, 0, C.c_void_p(16), None) == -6
+    assert lib.msf_power_accum_i32(h, C.c_void_p(16), 1, C.c_void_p(16), None) == -6
+    assert lib.msf_hist_sf_f32(h, C.c_void_p(16), 10, 1, None, 4, C.c_void_p(16), None) == -6
+    assert lib.msf_plan_status(h, None) == -6
+    assert lib.msf_plan_destroy(h) == 0
+
+
+def test_split_variant_for_odd_and_prime_sizes():
+    lib = mdsf.load()
+    for dims, variant in (((75, 81, 48), 2), ((64, 74, 26), 2), ((48, 48, 48), 1), ((512, 512, 512), 2)):
+        st, h = create(dims=dims)
+        assert st == 0
+        q = (C.c_int32 * 8)()
+        lib.msf_plan_query(h, q)
+        assert q[0] == variant, dims
+        lib.msf_plan_destroy(h)
+    st, h = create(dims=(75, 81, 48), variant=1)
+    assert st == -2
+
+
+def test_null_arguments():
+    lib = mdsf.load()
+    assert lib.msf_plan_create(None, None) == -1
+    assert lib.msf_hist_sf_f32(None, None, 0, 0, None, 0, None, None) == -1
+    assert lib.msf_sfplt(None, 4, 4, 3, None, None) == -1
+    assert lib.msf_sfplt(C.c_void_p(16), 5, 4, 3, C.c_void_p(16), None) == -2
+    assert lib.msf_ewald(None, 2, 2, 2, None, None, None, 1.0, None, None, None, None) == -1
+    assert lib.msf_direct_fwd(None, 10, None, 10, 0, 1, None, None, None) == -1
+    assert lib.msf_direct_bwd(None, 0, None, 0, 1, 1, None, None, None, None) == 0
+    assert lib.msf_gauss_grid_f64(None, None, None, 0, None, 1, None, None, None) == -1

@@ -1,0 +1,106 @@
+"""The drop-in compute_sf (Gaussian mode) against the reference's own outputs.
+
+The FP64 density (deposit + fold with the corner quirk) is compared at 1e-12
+relative to the oracle restatement; S(q) -- through the FP32 FFT -- at
+1e-5 * max(S) to the reference's saved arrays."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import mdsf
+from mdsf import dens as mdens
+from mdsf._lib import MsfError, c_p, call
+from conftest import GOLDEN
+from oracle import dens as odens
+
+pytestmark = pytest.mark.gpu
+NAMES = ["gauss_ortho", "gauss_tcl", "gauss_corner"]
+
+
+def case(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    rad = {str(n): (float(e), float(s)) for n, e, s in zip(z["rad_names"], z["rad_nel"], z["rad_sigma"])}
+    return z, rad
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_compute_sf_gauss_matches_reference(name, tmp_path):
+    z, rad = case(name)
+    r = z["r"].copy()
+    out = tmp_path / "out_sf"
+    mdens.compute_sf(r, z["L_in"].copy(), z["typ"].astype(object), str(out), rad, z["ucell"], float(z["Sres"]))
+    np.testing.assert_array_equal(r, z["r_after"])          # same in-place side effect
+    got = np.load(str(out) + ".npz")
+    assert sorted(got.files) == sorted(["sf", "sfplt", "L", "N", "kgrid", "kgridplt"])
+    for k in ("sf", "sfplt", "L", "N", "kgrid", "kgridplt"):
+        assert got[k].shape == z["out_" + k].shape and got[k].dtype == z["out_" + k].dtype, k
+    smax = z["out_sf"].max()
+    assert np.abs(got["sf"] - z["out_sf"]).max() < 1e-5 * smax
+    assert np.abs(got["sfplt"] - z["out_sfplt"]).max() < 1e-5 * smax
+    np.testing.assert_array_equal(got["kgrid"], z["out_kgrid"])
+    np.testing.assert_array_equal(got["kgridplt"][..., :3], z["out_kgridplt"][..., :3])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_gauss_density_fp64(name):
+    """The folded FP64 density of frame 0 against the oracle at 1e-12."""
+    z, rad = case(name)
+    r = z["r"].copy()
+    r, Lm = odens.rescale(r, z["L_in"].copy())
+    N = odens.grid_dims(Lm, float(z["Sres"]))
+    dr = Lm / N
+    odens.wrap(r, Lm)
+    typ = z["typ"].astype(object)
+    bdict, Nb = odens.borders(rad, dr, set(typ))
+    ref = odens.fold_tcl(odens.deposit_frame(r[0], typ, rad, bdict, Nb, N, dr, z["ucell"]), N, Nb)
+    names, tidx, tab, nb = mdens._type_table(rad, typ, dr)
+    assert nb == Nb
+    dims = tuple(int(n) for n in N)
+    plan = mdsf.get_plan(dims, Lm)
+    geom = np.zeros(16)
+    geom[0:3] = dr
+    geom[3:12] = z["ucell"].reshape(9)
+    geom[12] = nb
+    grid = torch.empty(dims, dtype=torch.float64, device="cuda")
+    rd = torch.from_numpy(np.ascontiguousarray(r[0])).cuda()
+    td = torch.from_numpy(tidx).cuda()
+    tabd = torch.from_numpy(tab).cuda()
+    call("msf_gauss_grid_f64", plan.handle, c_p(rd.data_ptr()), c_p(td.data_ptr()), len(tidx),
+         c_p(tabd.data_ptr()), len(names), c_p(geom.ctypes.data), c_p(grid.data_ptr()),
+         c_p(torch.cuda.current_stream().cuda_stream))
+    plan.status()
+    got = grid.cpu().numpy()
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def test_gauss_hist_mode_runs_and_matches_histogram(tmp_path):
+    z, rad = case("gauss_ortho")
+    out = mdens.compute_sf_arrays(z["r"].copy(), z["L_in"].copy(), z["typ"].astype(object), rad,
+                                  z["ucell"], float(z["Sres"]), mode="hist")
+    from oracle import hist as ohist
+    r = z["r"].copy()
+    r, Lm = odens.rescale(r, z["L_in"].copy())
+    odens.wrap(r, Lm)
+    w = np.array([int(rad[t][0]) for t in z["typ"]], np.int32)
+    ref = ohist.hist_sf(r, Lm, w, tuple(out["N"]))
+    assert np.abs(out["sf"] - ref).max() < 1e-5 * ref.max()
+
+
+def test_atom_outside_padded_grid_raises():
+    z, rad = case("gauss_ortho")
+    r = z["r"][:1].copy()
+    old = mdens.BUFFSIZE
+    mdens.BUFFSIZE = 10          # take the reference's buffered wrap branch: most atoms stay unwrapped
+    r[0, 20:] += 50.0
+    try:
+        with pytest.raises(MsfError, match="MSF_E_RANGE"):
+            mdens.compute_sf_arrays(r, z["L_in"][:1].copy(), z["typ"].astype(object), rad, z["ucell"],
+                                    float(z["Sres"]))
+    finally:
+        mdens.BUFFSIZE = old
+    # the plan's status word is cleared after the error is reported
+    mdens.compute_sf_arrays(z["r"][:1].copy(), z["L_in"][:1].copy(), z["typ"].astype(object), rad,
+                            z["ucell"], float(z["Sres"]))

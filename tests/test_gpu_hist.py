@@ -1,0 +1,119 @@
+"""Histogram deposit and the fused chain on the GPU against the oracle.
+
+Bar: the int32 grid is bit-exact with numpy.histogramdd; S(q) is within
+1e-5 * max(S) of the FP64 numpy path (FP32 FFT, FP64 frame sum)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import mdsf
+from mdsf import synth
+from conftest import GOLDEN
+from oracle import hist as ohist
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def test_hist_grid_golden_edges_all_layouts():
+    z = np.load(os.path.join(GOLDEN, "hist_edges.npz"))
+    dims, L, w = tuple(z["dims"]), z["L"], z["weights"]
+    g = mdsf.hist_grid(z["pos"], L, w, dims).cpu().numpy()
+    np.testing.assert_array_equal(g, z["grid"])
+    g32 = mdsf.hist_grid(z["pos32"], L, w, dims).cpu().numpy()
+    np.testing.assert_array_equal(g32, z["grid32"])
+    p4 = synth.pack_float4(z["pos32"], w)
+    g4 = mdsf.hist_grid(p4, L, None, dims).cpu().numpy()
+    np.testing.assert_array_equal(g4, z["grid32"])
+
+
+@pytest.mark.parametrize("dims,box", [((64, 64, 64), (2.5, 2.5, 2.5)), ((256, 256, 128), (16.0, 13.856, 8.0)),
+                                      ((75, 48, 81), (3.3, 4.1, 5.9)), ((2, 3, 5), (1.0, 1.0, 1.0))])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_hist_grid_random_outliers(dims, box, dtype):
+    rng = np.random.default_rng(11)
+    n = 50_000
+    box = np.asarray(box)
+    pos = (rng.uniform(-0.05, 1.05, (n, 3)) * box).astype(dtype)
+    pos[:50] = np.nan
+    pos[50:60] = box.astype(dtype)
+    pos[60:70, 0] = 0.0
+    w = rng.integers(1, 9, n).astype(np.int32)
+    ref = ohist.hist_grid(pos, box, w, dims)
+    got = mdsf.hist_grid(pos, box, w, dims).cpu().numpy()
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("wrap", [False, True])
+def test_hist_grid_scale_and_wrap(wrap):
+    rng = np.random.default_rng(5)
+    box = np.array([3.0, 2.0, 2.5])
+    pos = (rng.uniform(-0.3, 1.3, (20_000, 3)) * box).astype(np.float32)
+    w = rng.integers(1, 9, 20_000).astype(np.int32)
+    scale = np.array([1.01, 0.98, 1.003])
+    ref = ohist.hist_grid(pos, box, w, (40, 30, 36), scale_t=scale, wrap=wrap)
+    got = mdsf.hist_grid(pos, box, w, (40, 30, 36), scale=scale, wrap=wrap).cpu().numpy()
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_hist_sf_water_box_f64():
+    """Water box: 4,500 atoms, 2.5 nm, 64^3, 10 frames, float64 positions."""
+    pos, box, w = synth.water_box(frames=10)
+    ref = ohist.hist_sf(pos, box, w, (64, 64, 64))
+    got = mdsf.structure_factor(pos, box, w, (64, 64, 64)).cpu().numpy()
+    assert rel_err(got, ref) < TOL
+
+
+@pytest.mark.parametrize("layout", ["xyz", "float4"])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_hist_sf_columnar_headline_grid(layout, variant):
+    """Columnar system at the headline size (200k atoms, 256x256x128), 3 frames."""
+    pos, box, w = synth.columnar(frames=3)
+    ref = ohist.hist_sf(pos, box, w, (256, 256, 128))
+    arg = pos if layout == "xyz" else synth.pack_float4(pos, w)
+    got = mdsf.structure_factor(arg, box, w, (256, 256, 128), tuning=dict(variant=variant, batch=2)).cpu().numpy()
+    e = rel_err(got, ref)
+    rms = float(np.sqrt(np.mean((got - ref) ** 2)) / ref.max())
+    print(f"columnar {layout} variant {variant}: max err {e:.2e} rms {rms:.2e} of max(S)")
+    assert e < TOL
+
+
+def test_hist_sf_rescaled_frames_and_wrap():
+    rng = np.random.default_rng(9)
+    T, N = 4, 3000
+    boxes = np.array([[3.0, 3.2, 2.9]]) * (1 + 0.01 * rng.standard_normal((T, 1)))
+    pos = rng.uniform(-0.1, 1.1, (T, N, 3)) * boxes[:, None, :]
+    w = rng.integers(1, 9, N).astype(np.int32)
+    ref = ohist.hist_sf(pos, boxes, w, (32, 36, 30), wrap=True)
+    got = mdsf.structure_factor(pos, boxes, w, (32, 36, 30), wrap=True).cpu().numpy()
+    assert rel_err(got, ref) < TOL
+    got32 = mdsf.structure_factor(pos.astype(np.float32), boxes, w, (32, 36, 30), wrap=True).cpu().numpy()
+    ref32 = ohist.hist_sf(pos.astype(np.float32), boxes, w, (32, 36, 30), wrap=True)
+    assert rel_err(got32, ref32) < TOL
+
+
+def test_empty_and_mean():
+    box = np.array([1.0, 1.0, 1.0])
+    sf = mdsf.structure_factor(np.zeros((3, 0, 3), np.float32), box, np.zeros(0, np.int32), (8, 8, 8))
+    assert float(sf.abs().max()) == 0.0
+    pos, box, w = synth.uniform_system(100, (1.0, 1.0, 1.0), frames=4)
+    s1 = mdsf.structure_factor(pos, box, w, (8, 8, 8)).cpu().numpy()
+    s2 = mdsf.structure_factor(pos, box, w, (8, 8, 8), mean=True).cpu().numpy()
+    np.testing.assert_allclose(s2 * 4, s1, rtol=1e-12)
+    # accumulate into `out`, frame by frame == all frames at once
+    out = torch.zeros_like(torch.from_numpy(s1)).cuda()
+    for t in range(4):
+        mdsf.structure_factor(pos[t], box, w, (8, 8, 8), out=out)
+    np.testing.assert_allclose(out.cpu().numpy(), s1, rtol=1e-6)
+
+
+def test_single_atom_kat():
+    pos = np.array([[[0.31, 0.77, 0.12]]], np.float32)
+    sf = mdsf.structure_factor(pos, (1.0, 1.0, 1.0), np.array([7], np.int32), (16, 12, 10)).cpu().numpy()
+    np.testing.assert_allclose(sf, 49.0, rtol=1e-6)
