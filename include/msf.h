@@ -201,6 +201,28 @@ int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
                    int32_t q_shared, const float* g, const void* AB, void* grad,
                    msf_stream_t stream);
 
+/* ------------------------------------------- allocation-free chain variant
+ * No counterpart in the reference: an addition of this library for callers
+ * that may not allocate device memory (e.g. an MD engine calling analysis
+ * from inside its own memory pool, or a process under a hard device-memory
+ * quota).  Same result as msf_hist_sf_f32 (sf += the frame sum of
+ * |rfftn(histogram)|^2; pos_w device float4 (n_frames, n_atoms); box_host 3
+ * doubles in host memory), but the plan lives on the stack and the
+ * workspace is a fixed 32 MiB array inside the library image, which every
+ * GPU that loads libmsf.so holds until the process exits
+ * (msf_noalloc_scratch_bytes()).  Grids whose workspace does not fit
+ * (batch 1: 4*n0*n1*n2 + 8*n0*n1*(n2/2+1) bytes plus small tables; e.g.
+ * 128^3 fits, 256x256x128 does not) return MSF_E_WORKSPACE.  Nothing is
+ * allocated or freed.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and may load the module: make that
+ * first call before any stream capture.  Every call reuses the same array
+ * and re-initialises it, so calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller. */
+int msf_hist_sf_f32_noalloc(const void* pos_w, int64_t n_atoms, int64_t n_frames,
+                            const double* box_host, int32_t n0, int32_t n1, int32_t n2,
+                            int32_t flags, double* sf, msf_stream_t stream);
+size_t msf_noalloc_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -278,3 +278,11 @@ int msf_hist_sf_f64(msf_plan* p, const double* pos, const int32_t* weights, int6
 }
 
 }  // extern "C"
+
+// The chain for callers inside the library that hold their own plan.
+int msf::hist_sf_chain(msf_plan* p, const void* pos, const int32_t* weights, int layout,
+                       int64_t n_atoms, int64_t n_frames, const double* scale, int32_t flags,
+                       double* sf, cudaStream_t st) {
+  return hist_sf_any(p, pos, weights, layout, n_atoms, n_frames, scale, flags, sf,
+                     reinterpret_cast<msf_stream_t>(st));
+}

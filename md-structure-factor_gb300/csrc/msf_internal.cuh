@@ -250,6 +250,12 @@ __device__ __forceinline__ void copy_table(T* dst, const T* __restrict__ src, in
   for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
+// Fills a caller-owned plan from a descriptor (host only, no allocation).
+int plan_init(msf_plan* p, const msf_plan_desc* d);
+// The chain of msf_hist_sf_* over one position layout (msf_hist.cu).
+int hist_sf_chain(msf_plan* p, const void* pos, const int32_t* weights, int layout, int64_t n_atoms,
+                  int64_t n_frames, const double* scale, int32_t flags, double* sf, cudaStream_t st);
+
 // Launch helpers implemented in msf_fft.cu, used by the chain entry points.
 int fft_power_batch(msf_plan* p, const void* grids, int grid_kind, int nframes, double* sf,
                     int zero_grids, cudaStream_t st);

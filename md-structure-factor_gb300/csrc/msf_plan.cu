@@ -120,6 +120,19 @@ int msf_version(void) { return 100; }
 int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
   if (!out || !d) return MSF_E_INVALID;
   *out = nullptr;
+  msf_plan* p = new (std::nothrow) msf_plan;
+  if (!p) return MSF_E_INVALID;
+  const int s = msf::plan_init(p, d);
+  if (s) { delete p; return s; }
+  *out = p;
+  return MSF_OK;
+}
+
+}  // extern "C"
+
+// Fills *p from *d (host only, no allocation).  Shared by msf_plan_create
+// and by the entry points that keep their plan on the stack.
+int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   const int n[3] = {d->n0, d->n1, d->n2};
   for (int i = 0; i < 3; ++i)
     if (n[i] < 2 || n[i] > kMaxN) return MSF_E_UNSUPPORTED;
@@ -129,8 +142,6 @@ int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
   if (d->variant < 0 || d->variant > 2) return MSF_E_INVALID;
   if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
-  msf_plan* p = new (std::nothrow) msf_plan;
-  if (!p) return MSF_E_INVALID;
   memset(p, 0, sizeof(*p));
   p->n0 = n[0]; p->n1 = n[1]; p->n2 = n[2];
   p->nh = n[2] / 2 + 1;
@@ -147,7 +158,7 @@ int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
                         plane_smem <= 220 * 1024;
   int variant = d->variant;
   if (variant == 0) variant = plane_ok ? 1 : 2;
-  if (variant == 1 && !plane_ok) { delete p; return MSF_E_UNSUPPORTED; }
+  if (variant == 1 && !plane_ok) return MSF_E_UNSUPPORTED;
   p->variant = variant;
   p->plane_smem = plane_smem;
   p->plane_threads = (n[2] * P >= 8192) ? 512 : 256;
@@ -159,7 +170,7 @@ int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
     while (w > 4 && nmax * w > 4096) w /= 2;
     while (w < 32 && nmax * w * 2 <= 4096) w *= 2;
   }
-  if ((size_t)(n[0] > n[1] ? n[0] : n[1]) * w > 4096) { delete p; return MSF_E_UNSUPPORTED; }
+  if ((size_t)(n[0] > n[1] ? n[0] : n[1]) * w > 4096) return MSF_E_UNSUPPORTED;
   p->tile_w = w;
   int g = d->rows_per_block;
   if (g == 0) {
@@ -167,10 +178,10 @@ int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
     if (g < 2) g = 2;
     if (g > 32) g = 32;
   }
-  if (g < 1 || g > 64) { delete p; return MSF_E_INVALID; }
+  if (g < 1 || g > 64) return MSF_E_INVALID;
   p->rows_per_block = g;
   p->deposit_block = d->deposit_block ? d->deposit_block : 256;
-  if (p->deposit_block % 32 || p->deposit_block > 1024) { delete p; return MSF_E_INVALID; }
+  if (p->deposit_block % 32 || p->deposit_block > 1024) return MSF_E_INVALID;
 
   // workspace layout
   size_t o = 0;
@@ -186,9 +197,10 @@ int msf_plan_create(msf_plan** out, const msf_plan_desc* d) {
   p->off_grid = o; o = align_up(o + (size_t)p->batch * grid_elems(p) * sizeof(int32_t));
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
   p->ws_bytes = o;
-  *out = p;
   return MSF_OK;
 }
+
+extern "C" {
 
 int msf_plan_destroy(msf_plan* p) {
   delete p;

@@ -68,6 +68,8 @@ SIGNATURES = {
     "msf_ewald": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_d, c_p, c_p, c_p, c_p]),
     "msf_direct_fwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p]),
     "msf_direct_bwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p, c_p]),
+    "msf_hist_sf_f32_noalloc": (c_int, [c_p, c_i64, c_i64, c_p, c_int, c_int, c_int, c_int, c_p, c_p]),
+    "msf_noalloc_scratch_bytes": (c_size, []),
 }
 
 
