@@ -218,7 +218,7 @@ def main():
     if not tuning:
         from mdsf import tune
         tuning = tune.lookup(DIMS) or {"batch": 8}
-    plan = mdsf.get_plan(DIMS, box, device=dev, **tuning)
+    plan = mdsf.get_plan(DIMS, box, device=dev, max_atoms=N_ATOMS, **tuning)
     st = torch.cuda.current_stream(dev)
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=dev)
     X, Y, Z = mdsf.plot_axes(plan.half_shape, box)
@@ -239,7 +239,7 @@ def main():
              _ptr(ew[0]), _ptr(ew[1]), _ptr(ew[2]), sp)
 
     batches = (FRAMES + plan.batch - 1) // plan.batch
-    launches_per_step = batches * (3 if plan.variant == 1 else 4) + 2
+    launches_per_step = batches * {1: 3, 2: 4, 3: 5}[plan.variant] + 2
 
     # warm-up (also primes one-time kernel attributes before graph capture)
     for _ in range(2):
@@ -323,12 +323,21 @@ def main():
     Vh = DIMS[0] * DIMS[1] * plan.nh
     B = plan.batch
     # compulsory bytes of each stage for one launch of `B` frames
-    stage_bytes = {
-        1: lambda k: 16 * N_ATOMS * k + 4 * V * k,                 # positions read, grid written
-        2: lambda k: 4 * V * k + 4 * V * k + 8 * Vh * k,            # grid read, grid zeroed, spectrum written
-        4: lambda k: 8 * Vh * k + 16 * Vh,                          # spectrum read, sf read + written
-    }
-    stage_names = {1: "k_hist_deposit", 2: "k_plane" if plan.variant == 1 else "k_zrows+k_ycols", 4: "k_xpower"}
+    if plan.variant == 3:
+        stage_bytes = {
+            1: lambda k: 2 * 16 * N_ATOMS * k + 8 * N_ATOMS * k,   # positions read twice, bucket written
+            2: lambda k: 8 * N_ATOMS * k + 8 * Vh * k,              # bucket read, spectrum written
+            4: lambda k: 8 * Vh * k + 16 * Vh,                      # spectrum read, sf read + written
+        }
+        stage_names = {1: "k_bucket_count+scan+fill", 2: "k_plane_ct", 4: "k_xpower_ct"}
+    else:
+        stage_bytes = {
+            1: lambda k: 16 * N_ATOMS * k + 4 * V * k,             # positions read, grid written
+            2: lambda k: 4 * V * k + 4 * V * k + 8 * Vh * k,        # grid read, grid zeroed, spectrum written
+            4: lambda k: 8 * Vh * k + 16 * Vh,                      # spectrum read, sf read + written
+        }
+        stage_names = {1: "k_hist_deposit", 2: "k_plane" if plan.variant == 1 else "k_zrows+k_ycols",
+                       4: "k_xpower"}
     totals = {s: sum(t for t, _ in v) for s, v in stage_ms.items()}
     dom = max(totals, key=totals.get)
     full = [(t, k) for t, k in stage_ms[dom] if k == B] or stage_ms[dom]
@@ -386,7 +395,7 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     from mdsf._lib import c_p, call
     from mdsf.api import _ptr
     out = {}
-    plan1 = mdsf.get_plan(DIMS, box, device=dev, batch=1)
+    plan1 = mdsf.get_plan(DIMS, box, device=dev, batch=1, max_atoms=N_ATOMS)
     sf = torch.zeros(plan1.half_shape, dtype=torch.float64, device=dev)
     st = torch.cuda.current_stream(dev)
 

@@ -66,10 +66,14 @@ typedef struct msf_plan_desc {
   int32_t n0, n1, n2;     /* grid; each in [2, 1024] */
   int32_t batch;          /* frames per batch (>=1); 0 = default */
   double box[3];          /* box edges L used for binning (mean box when frames are rescaled) */
-  int32_t variant;        /* FFT variant: 0 auto, 1 fused z+y plane, 2 split rows/cols */
+  int32_t variant;        /* 0 auto, 1 z+y plane from a global grid, 2 split rows/cols,
+                             3 bucketed: atoms binned per x-plane and deposited in shared
+                             memory by the plane FFT kernel (power-of-two grids) */
   int32_t tile_w;         /* columns per x-pass tile: 0 auto, else 4..32 */
   int32_t rows_per_block; /* row pairs per z-pass block: 0 auto */
   int32_t deposit_block;  /* threads per deposit block: 0 auto */
+  int64_t max_atoms;      /* atoms per frame the chain may be called with (sizes the per-plane
+                             atom buckets of variant 3); 0 = no buckets */
 } msf_plan_desc;
 
 int msf_plan_create(msf_plan** plan, const msf_plan_desc* desc);
@@ -78,7 +82,8 @@ size_t msf_plan_workspace_bytes(const msf_plan* plan);
 int msf_plan_bind(msf_plan* plan, void* workspace, size_t workspace_bytes, msf_stream_t stream);
 /* Synchronises `stream`, returns and clears the device status word. */
 int msf_plan_status(msf_plan* plan, msf_stream_t stream);
-/* Effective tuning of a plan: variant, tile_w, rows_per_block, batch. */
+/* Effective tuning of a plan: variant, tile_w, rows_per_block, batch,
+ * deposit_block, plane_threads, x pass fed by TMA (0/1), nh. */
 int msf_plan_query(const msf_plan* plan, int32_t out[8]);
 
 /* ------------------------------------------------ histogram deposit (a5)
@@ -137,6 +142,14 @@ int msf_hist_sf_f32xyz(msf_plan* plan, const float* pos, const int32_t* weights,
 int msf_hist_batch_stages(msf_plan* plan, int32_t stages, int32_t layout, const void* pos,
                           const int32_t* weights, int64_t n_atoms, int32_t n_frames,
                           const double* scale, int32_t flags, double* sf, msf_stream_t stream);
+/* Verification view of the bucketed variant (variant 3): bins one frame
+ * into the per-x-plane atom lists exactly as msf_hist_sf_* does and adds
+ * them into the caller's int32 grid (`grid += histogram`), so the in-chain
+ * binning can be compared with numpy.histogramdd bit for bit.  Layouts as
+ * msf_hist_batch_stages. */
+int msf_hist_bucket_grid(const msf_plan* plan, int32_t layout, const void* pos,
+                         const int32_t* weights, int64_t n_atoms, const double* scale,
+                         int32_t flags, int32_t* grid, msf_stream_t stream);
 /* pos: (n_frames, n_atoms, 3) doubles, weights: (n_atoms) int32. */
 int msf_hist_sf_f64(msf_plan* plan, const double* pos, const int32_t* weights, int64_t n_atoms,
                     int64_t n_frames, const double* scale, int32_t flags, double* sf,

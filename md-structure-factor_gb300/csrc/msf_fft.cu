@@ -385,6 +385,8 @@ static int stage_a_kind(msf_plan* p, const void* grids, int nframes, int zero, c
 
 int fft_stage_a(msf_plan* p, const void* grids, int kind, int nframes, int zero, cudaStream_t st) {
   if (nframes < 1 || nframes > p->batch) return MSF_E_INVALID;
+  // bucketed plans read caller grids with the compile-time plane kernel (never zeroing them)
+  if (p->variant == 3) return fused_plane_batch(p, grids, kind, nframes, st);
   switch (kind) {
     case kGridI32: return stage_a_kind<kGridI32>(p, grids, nframes, zero, st);
     case kGridF32: return stage_a_kind<kGridF32>(p, grids, nframes, zero, st);
@@ -394,6 +396,7 @@ int fft_stage_a(msf_plan* p, const void* grids, int kind, int nframes, int zero,
 
 int fft_stage_b(msf_plan* p, int nframes, double* sf, cudaStream_t st) {
   if (nframes < 1 || nframes > p->batch) return MSF_E_INVALID;
+  if (p->variant == 3) return fused_x_batch(p, nframes, sf, st);
   return launch_xpower(p, nframes, sf, st);
 }
 

@@ -20,61 +20,9 @@
 // Deposit: one atom per thread, float4 (x, y, z, w) loads, voxels of a warp
 // matched with __match_any_sync and summed with __reduce_add_sync so that a
 // voxel hit by several lanes takes one atomicAdd.
-#include "msf_internal.cuh"
+#include "msf_bins.cuh"
 
 namespace msf {
-
-struct DepArgs {
-  const void* pos;
-  const int32_t* w;
-  int64_t n_atoms;
-  int64_t frame_stride;  // elements (float4 or double) between frames
-  const double* scale;   // (nframes, 3) or null
-  int flags;
-  int n0, n1, n2;
-  double L0, L1, L2;
-  float inv0, inv1, inv2;
-  const double* e0;
-  const double* e1;
-  const double* e2;
-  const float* flo0;
-  const float* flo1;
-  const float* flo2;
-  const float* fhi0;
-  const float* fhi1;
-  const float* fhi2;
-  int32_t* grids;
-  int64_t V;
-};
-
-__device__ __forceinline__ int bin_f32(float x, int n, float inv, const float* __restrict__ flo,
-                                       const float* __restrict__ fhi) {
-  if (!(x >= __ldg(flo)) || !(x <= __ldg(fhi + n))) return -1;  // also drops NaN
-  int b = (int)(x * inv);
-  b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
-  while (b > 0 && x < __ldg(flo + b)) --b;
-  while (b < n - 1 && x >= __ldg(flo + b + 1)) ++b;
-  return b;
-}
-
-__device__ __forceinline__ int bin_f64(double x, int n, float inv, const double* __restrict__ e) {
-  if (!(x >= __ldg(e)) || !(x <= __ldg(e + n))) return -1;
-  int b = (int)((float)x * inv);
-  b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
-  while (b > 0 && x < __ldg(e + b)) --b;
-  while (b < n - 1 && x >= __ldg(e + b + 1)) ++b;
-  return b;
-}
-
-// dens.py:52-58 (per-frame rescale) and dens.py:211-212 (wrap), in FP64.
-__device__ __forceinline__ double prep(double x, const double* s, int axis, bool wrap, double L) {
-  if (s) x = __dmul_rn(x, __ldg(s + axis));
-  if (wrap) {
-    x = (x < L) ? x : __dsub_rn(x, L);
-    x = (x > 0.0) ? x : __dadd_rn(x, L);
-  }
-  return x;
-}
 
 // MODE 0: float4, FP32 binning; 1: float4, FP64 rescale/wrap; 2: FP64 (N,3) + int32 weights;
 // 3: float (N,3) + int32 weights, FP32 binning; 4: float (N,3) + int32 weights, FP64 rescale/wrap
@@ -128,24 +76,6 @@ __global__ void k_hist_deposit(DepArgs a) {
     const int sum = __reduce_add_sync(peers, wgt);
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(a.grids + key, sum);
   }
-}
-
-static DepArgs dep_args(const msf_plan* p) {
-  DepArgs a;
-  a.n0 = p->n0; a.n1 = p->n1; a.n2 = p->n2;
-  a.L0 = p->box[0]; a.L1 = p->box[1]; a.L2 = p->box[2];
-  a.inv0 = (float)(p->n0 / p->box[0]);
-  a.inv1 = (float)(p->n1 / p->box[1]);
-  a.inv2 = (float)(p->n2 / p->box[2]);
-  const double* e = ws_ptr<double>(p, p->off_edges_d);
-  const float* lo = ws_ptr<float>(p, p->off_edges_flo);
-  const float* hi = ws_ptr<float>(p, p->off_edges_fhi);
-  const int o1 = p->n0 + 1, o2 = p->n0 + p->n1 + 2;
-  a.e0 = e; a.e1 = e + o1; a.e2 = e + o2;
-  a.flo0 = lo; a.flo1 = lo + o1; a.flo2 = lo + o2;
-  a.fhi0 = hi; a.fhi1 = hi + o1; a.fhi2 = hi + o2;
-  a.V = grid_elems(p);
-  return a;
 }
 
 int hist_deposit_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
@@ -226,13 +156,21 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
   const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
   const size_t esize = layout == kLayoutF32x4 ? 4 * sizeof(float)
                        : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
+  if (p->variant == 3 && n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
   for (int64_t f = 0; f < n_frames; f += p->batch) {
     const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
     const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;
-    int s = hist_deposit_batch(p, fp, weights, layout, n_atoms, nb, fstride,
-                               scale ? scale + 3 * f : nullptr, flags, grids, st);
-    if (s) return s;
-    s = fft_power_batch(p, grids, kGridI32, nb, sf, 1, st);
+    int s;
+    if (p->variant == 3) {
+      s = fused_bucket_batch(p, fp, weights, layout, n_atoms, nb, fstride,
+                             scale ? scale + 3 * f : nullptr, flags, st);
+      if (!s) s = fused_plane_batch(p, nullptr, kGridI32, nb, st);
+      if (!s) s = fused_x_batch(p, nb, sf, st);
+    } else {
+      s = hist_deposit_batch(p, fp, weights, layout, n_atoms, nb, fstride,
+                             scale ? scale + 3 * f : nullptr, flags, grids, st);
+      if (!s) s = fft_power_batch(p, grids, kGridI32, nb, sf, 1, st);
+    }
     if (s) return s;
   }
   return MSF_OK;
@@ -262,11 +200,15 @@ int msf_hist_batch_stages(msf_plan* p, int32_t stages, int32_t layout, const voi
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
   int s = MSF_OK;
+  const bool bucketed = p->variant == 3;
   if (stages & 1) {
     const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
-    s = hist_deposit_batch(p, pos, weights, layout, n_atoms, n_frames, fstride, scale, flags, grids, st);
+    s = bucketed ? fused_bucket_batch(p, pos, weights, layout, n_atoms, n_frames, fstride, scale, flags, st)
+                 : hist_deposit_batch(p, pos, weights, layout, n_atoms, n_frames, fstride, scale, flags, grids, st);
   }
-  if (!s && (stages & 2)) s = fft_stage_a(p, grids, kGridI32, n_frames, 1, st);
+  if (!s && (stages & 2))
+    s = bucketed ? fused_plane_batch(p, nullptr, kGridI32, n_frames, st)
+                 : fft_stage_a(p, grids, kGridI32, n_frames, 1, st);
   if (!s && (stages & 4)) s = fft_stage_b(p, n_frames, sf, st);
   return s;
 }

@@ -54,6 +54,12 @@ struct msf_plan {
   char* ws;
   int bound;
   size_t plane_smem;     // dynamic smem of the fused plane kernel
+  // bucketed chain (variant 3): per-x-plane atom lists
+  int64_t max_atoms;
+  size_t off_counts, off_offsets, off_cursor, off_bucket;
+  // TMA tensor map over the spectra for the x pass (CUtensorMap, 128 bytes)
+  alignas(64) unsigned char xtma_map[128];
+  int xtma_ready;
 };
 
 namespace msf {
@@ -255,6 +261,22 @@ int plan_init(msf_plan* p, const msf_plan_desc* d);
 // The chain of msf_hist_sf_* over one position layout (msf_hist.cu).
 int hist_sf_chain(msf_plan* p, const void* pos, const int32_t* weights, int layout, int64_t n_atoms,
                   int64_t n_frames, const double* scale, int32_t flags, double* sf, cudaStream_t st);
+
+// Bucketed chain for power-of-two grids (msf_fused.cu).
+bool ct_plane_ok(int n1, int n2);
+int ct_x_width(int n0, int requested);   // 0 when no x kernel exists for n0 (and width)
+size_t ct_plane_smem(int n1, int n2);
+int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
+                       int64_t n_atoms, int nframes, int64_t frame_stride, const double* scale,
+                       int flags, cudaStream_t st);
+int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st);
+int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
+// x pass with TMA tile loads (msf_xtma.cu); prepared at bind time
+bool xtma_ok(int n0, int w);
+int xtma_prepare(msf_plan* p);
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
+int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int layout, int64_t n_atoms,
+                const double* scale, int flags, int32_t* grid, cudaStream_t st);
 
 // Launch helpers implemented in msf_fft.cu, used by the chain entry points.
 int fft_power_batch(msf_plan* p, const void* grids, int grid_kind, int nframes, double* sf,

@@ -139,7 +139,8 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   for (int i = 0; i < 3; ++i)
     if (!(d->box[i] > 0.0) || !isfinite(d->box[i])) return MSF_E_INVALID;
   if (d->batch < 0 || d->batch > 256) return MSF_E_INVALID;
-  if (d->variant < 0 || d->variant > 2) return MSF_E_INVALID;
+  if (d->variant < 0 || d->variant > 3) return MSF_E_INVALID;
+  if (d->max_atoms < 0) return MSF_E_INVALID;
   if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
   memset(p, 0, sizeof(*p));
@@ -156,9 +157,12 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   const size_t plane_smem = (size_t)n[2] * SP * sizeof(float2) + (size_t)(n[2] + P) * (sizeof(float2) + sizeof(int));
   const bool plane_ok = (n[1] % 2 == 0) && P >= 2 && !p->ax[2].generic && !p->axp.generic &&
                         plane_smem <= 220 * 1024;
+  const bool fused_ok = ct_plane_ok(n[1], n[2]) && ct_x_width(n[0], d->tile_w) > 0 && n[0] <= kMaxN;
   int variant = d->variant;
-  if (variant == 0) variant = plane_ok ? 1 : 2;
+  if (variant == 0) variant = fused_ok ? 3 : (plane_ok ? 1 : 2);
   if (variant == 1 && !plane_ok) return MSF_E_UNSUPPORTED;
+  if (variant == 3 && !fused_ok) return MSF_E_UNSUPPORTED;
+  p->max_atoms = d->max_atoms;
   p->variant = variant;
   p->plane_smem = plane_smem;
   p->plane_threads = (n[2] * P >= 8192) ? 512 : 256;
@@ -172,6 +176,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   }
   if ((size_t)(n[0] > n[1] ? n[0] : n[1]) * w > 4096) return MSF_E_UNSUPPORTED;
   p->tile_w = w;
+  if (variant == 3) p->tile_w = ct_x_width(n[0], d->tile_w);
   int g = d->rows_per_block;
   if (g == 0) {
     g = 2048 / n[2];
@@ -194,7 +199,12 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   p->off_edges_d = o; o = align_up(o + ne * sizeof(double));
   p->off_edges_flo = o; o = align_up(o + ne * sizeof(float));
   p->off_edges_fhi = o; o = align_up(o + ne * sizeof(float));
-  p->off_grid = o; o = align_up(o + (size_t)p->batch * grid_elems(p) * sizeof(int32_t));
+  // density grids: the bucketed variant never materialises them
+  p->off_grid = o; o = align_up(o + (variant == 3 ? 0 : (size_t)p->batch * grid_elems(p) * sizeof(int32_t)));
+  p->off_counts = o; o = align_up(o + (size_t)p->batch * n[0] * sizeof(int));
+  p->off_offsets = o; o = align_up(o + (size_t)p->batch * (n[0] + 1) * sizeof(int));
+  p->off_cursor = o; o = align_up(o + (size_t)p->batch * n[0] * sizeof(int));
+  p->off_bucket = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * p->max_atoms * 8 : 0));
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
   p->ws_bytes = o;
   return MSF_OK;
@@ -234,8 +244,14 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
   k_init_tables<<<8, 256, 0, st>>>(a);
   int s = launch_status();
   if (s) return s;
-  s = cuda_status(cudaMemsetAsync(p->ws + p->off_grid, 0,
-                                  (size_t)p->batch * grid_elems(p) * sizeof(int32_t), st));
+  if (p->variant != 3) {
+    s = cuda_status(cudaMemsetAsync(p->ws + p->off_grid, 0,
+                                    (size_t)p->batch * grid_elems(p) * sizeof(int32_t), st));
+    if (s) return s;
+  }
+  s = cuda_status(cudaMemsetAsync(p->ws + p->off_counts, 0, (size_t)p->batch * p->n0 * sizeof(int), st));
+  if (s) return s;
+  s = xtma_prepare(p);
   if (s) return s;
   p->bound = 1;
   return MSF_OK;
@@ -264,7 +280,7 @@ int msf_plan_query(const msf_plan* p, int32_t out[8]) {
   out[3] = p->batch;
   out[4] = p->deposit_block;
   out[5] = p->plane_threads;
-  out[6] = (int32_t)(p->ws_bytes >> 20);
+  out[6] = p->xtma_ready;
   out[7] = p->nh;
   return MSF_OK;
 }

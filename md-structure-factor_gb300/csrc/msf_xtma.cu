@@ -1,0 +1,258 @@
+// msf_xtma.cu -- x pass of the bucketed chain with TMA tile loads.
+//
+// The half spectra of a batch are one row-major matrix of B*n0 rows (frame,
+// x) by F = n1*(n2/2+1) complex columns.  A persistent CTA walks work items
+// (column tile of W columns, frame); each item's (n0 x W) tile is fetched by
+// cp.async.bulk.tensor.2d into one of two shared-memory buffers and tracked
+// by an mbarrier, so the copy of item s+1 (and s+2) runs while item s is
+// transformed.  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed
+// over the frames of the tile in FP32, one FP64 read-modify-write of sf per
+// tile.  Waits are bounded: on timeout the kernel latches MSF_E_TIMEOUT in
+// the plan status word and returns.
+#include <cuda.h>
+
+#include "msf_ct.cuh"
+
+namespace msf {
+
+struct XTmaArgs {
+  int nframes;
+  int64_t F;
+  int ntiles;
+  double* sf;
+  const float2* twx;
+  int* status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// true when the phase with the given parity has completed
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+constexpr long long kWaitLimit = 1LL << 26;  // try_wait polls before giving up (seconds)
+
+template <int N0, int W>
+struct XTmaShape {
+  static constexpr int NT = 256;
+  static constexpr int EPT = N0 * W / NT;
+  static constexpr int BOX_ROWS = N0 <= 256 ? N0 : 256;
+  static constexpr int NBOX = N0 / BOX_ROWS;
+  static constexpr uint32_t TILE_BYTES = N0 * W * sizeof(float2);
+  static constexpr size_t SMEM = 1024 + 2 * (size_t)TILE_BYTES + N0 * sizeof(float2);
+};
+
+template <int N0, int W>
+__global__ void __launch_bounds__(256) k_xpower_tma(const __grid_constant__ CUtensorMap map, XTmaArgs a) {
+  using S = XTmaShape<N0, W>;
+  constexpr int NT = S::NT, EPT = S::EPT;
+  static_assert(EPT * NT == N0 * W, "tile must split evenly over the threads");
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int abort_flag;
+  // 1024-byte aligned tile buffers (TMA destination)
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  float2* buf0 = reinterpret_cast<float2*>(base);
+  float2* buf1 = buf0 + N0 * W;
+  float2* tw = buf1 + N0 * W;
+  const int tid = threadIdx.x;
+  const int my_tiles = (a.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int total = my_tiles > 0 ? my_tiles * a.nframes : 0;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < N0; i += NT) tw[i] = a.twx[i];
+  __syncthreads();
+
+  auto issue = [&](int s) {
+    const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
+    const int frame = s % a.nframes;
+    float2* dst = (s & 1) ? buf1 : buf0;
+    uint64_t* b = &bar[s & 1];
+    mbar_expect_tx(b, S::TILE_BYTES);
+#pragma unroll
+    for (int k = 0; k < S::NBOX; ++k)
+      tma_load_2d(dst + k * S::BOX_ROWS * W, &map, tile * W, frame * N0 + k * S::BOX_ROWS, b);
+  };
+  if (tid == 0) {
+    if (total > 0) issue(0);
+    if (total > 1) issue(1);
+  }
+  uint32_t phase0 = 0, phase1 = 0;
+  int pos_x[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    const int e = tid + i * NT;
+    pos_x[i] = ct::pos<N0>(e / W) * W + (e % W);
+  }
+  float acc[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) acc[i] = 0.f;
+
+  for (int s = 0; s < total; ++s) {
+    const int b = s & 1;
+    uint64_t* bb = &bar[b];
+    const uint32_t par = b ? phase1 : phase0;
+    long long spins = 0;
+    while (!mbar_try_wait(bb, par)) {
+      if (++spins > kWaitLimit) { atomicExch(&abort_flag, 1); break; }
+    }
+    __syncthreads();
+    if (abort_flag) {
+      if (tid == 0) atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
+      break;
+    }
+    if (b) phase1 ^= 1u; else phase0 ^= 1u;
+    float2* t = b ? buf1 : buf0;
+    ct::dif<N0, W, W, 1, NT, true>(t, tw);
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const float2 v = t[pos_x[i]];
+      acc[i] = fmaf(v.x, v.x, fmaf(v.y, v.y, acc[i]));
+    }
+    const int frame = s % a.nframes;
+    if (frame == a.nframes - 1) {
+      const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
+      const int64_t f0 = (int64_t)tile * W;
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int e = tid + i * NT;
+        const int x = e / W, w = e % W;
+        if (f0 + w < a.F) {
+          double* d = a.sf + (int64_t)x * a.F + f0 + w;
+          *d = *d + (double)acc[i];
+        }
+        acc[i] = 0.f;
+      }
+    }
+    __syncthreads();   // every thread is done with buffer b
+    if (tid == 0 && s + 2 < total) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(s + 2);
+    }
+  }
+  // leave no copy in flight into this CTA's shared memory (bounded)
+  if (tid == 0 && abort_flag) {
+    for (int k = 0; k < 2; ++k) {
+      long long spins = 0;
+      while (!mbar_try_wait(&bar[k], k ? phase1 : phase0) && ++spins < kWaitLimit) {
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- host side
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+template <int N0, int W>
+static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs& a, cudaStream_t st) {
+  using S = XTmaShape<N0, W>;
+  static int grid = 0;
+  if (!grid) {
+    cudaFuncSetAttribute(k_xpower_tma<N0, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_xpower_tma<N0, W>, S::NT, S::SMEM);
+    grid = (sms > 0 ? sms : 152) * (occ > 0 ? occ : 1);
+  }
+  const int g = a.ntiles < grid ? a.ntiles : grid;
+  k_xpower_tma<N0, W><<<g, S::NT, S::SMEM, st>>>(*map, a);
+  return launch_status();
+}
+
+#define MSF_XTMA_CASES(X) X(64, 32) X(128, 16) X(128, 32) X(256, 16) X(256, 8) X(512, 8)
+
+bool xtma_ok(int n0, int w) {
+#define X(A, B) if (n0 == A && w == B) return true;
+  MSF_XTMA_CASES(X)
+#undef X
+  return false;
+}
+
+// Encodes the tensor map over the plan's spectra (after msf_plan_bind).
+int xtma_prepare(msf_plan* p) {
+  p->xtma_ready = 0;
+  if (p->variant != 3 || !xtma_ok(p->n0, p->tile_w)) return MSF_OK;
+  const int64_t F = (int64_t)p->n1 * p->nh;
+  if ((F * sizeof(float2)) % 16 || (p->tile_w % 2)) return MSF_OK;
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return MSF_OK;
+  const int box_rows = p->n0 <= 256 ? p->n0 : 256;
+  cuuint64_t dims[2] = {(cuuint64_t)F, (cuuint64_t)p->batch * p->n0};
+  cuuint64_t strides[1] = {(cuuint64_t)(F * sizeof(float2))};
+  cuuint32_t box[2] = {(cuuint32_t)p->tile_w, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUtensorMap* m = reinterpret_cast<CUtensorMap*>(p->xtma_map);
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, p->ws + p->off_cplx, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return MSF_OK;   // plain loads then
+  p->xtma_ready = 1;
+  return MSF_OK;
+}
+
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
+  XTmaArgs a;
+  a.nframes = nframes;
+  a.F = (int64_t)p->n1 * p->nh;
+  a.ntiles = (int)((a.F + p->tile_w - 1) / p->tile_w);
+  a.sf = sf;
+  a.twx = ws_ptr<float2>(p, p->off_tw[0]);
+  a.status = ws_ptr<int>(p, p->off_status);
+  const CUtensorMap* map = reinterpret_cast<const CUtensorMap*>(p->xtma_map);
+#define X(A, B) if (p->n0 == A && p->tile_w == B) return launch_xtma<A, B>(p, map, a, st);
+  MSF_XTMA_CASES(X)
+#undef X
+  return MSF_E_UNSUPPORTED;
+}
+
+}  // namespace msf

@@ -40,7 +40,7 @@ class MsfError(RuntimeError):
 class PlanDesc(C.Structure):
     _fields_ = [("n0", c_int), ("n1", c_int), ("n2", c_int), ("batch", c_int),
                 ("box", c_d * 3), ("variant", c_int), ("tile_w", c_int),
-                ("rows_per_block", c_int), ("deposit_block", c_int)]
+                ("rows_per_block", c_int), ("deposit_block", c_int), ("max_atoms", c_i64)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/msf.h
@@ -62,6 +62,7 @@ SIGNATURES = {
     "msf_hist_sf_f32": (c_int, [c_p, c_p, c_i64, c_i64, c_p, c_int, c_p, c_p]),
     "msf_hist_sf_f32xyz": (c_int, [c_p, c_p, c_p, c_i64, c_i64, c_p, c_int, c_p, c_p]),
     "msf_hist_sf_f64": (c_int, [c_p, c_p, c_p, c_i64, c_i64, c_p, c_int, c_p, c_p]),
+    "msf_hist_bucket_grid": (c_int, [c_p, c_int, c_p, c_p, c_i64, c_p, c_int, c_p, c_p]),
     "msf_hist_batch_stages": (c_int, [c_p, c_int, c_int, c_p, c_p, c_i64, c_int, c_p, c_int, c_p, c_p]),
     "msf_gauss_grid_f64": (c_int, [c_p, c_p, c_p, c_i64, c_p, c_int, c_p, c_p, c_p]),
     "msf_sfplt": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p]),

@@ -102,7 +102,9 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
         pos = pos[None]
     T, N, C = pos.shape
     scale, L = frame_scale(box)
-    plan = get_plan(grid_dims, L, device=device, **(tuning or {}))
+    kw = dict(tuning or {})
+    kw.setdefault("max_atoms", N)
+    plan = get_plan(grid_dims, L, device=device, **kw)
     if out is None:
         sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=device)
     else:

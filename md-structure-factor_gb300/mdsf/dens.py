@@ -155,7 +155,7 @@ def compute_sf_arrays(r, L, typ, rad, ucell, Sres, mode="gauss", device=None):
     if PRINT_DETAILS:
         print("Using a spatial grid of: %s, actual resolution %s" % (N, Lm / N))
     dims = tuple(int(n) for n in N)
-    plan = get_plan(dims, Lm, device=device)
+    plan = get_plan(dims, Lm, device=device, max_atoms=r.shape[1])
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=device)
     T, nat = r.shape[0], r.shape[1]
     with torch.cuda.device(device):

@@ -16,7 +16,7 @@ import torch
 from . import _lib
 from ._lib import c_p, call, load
 
-VARIANTS = {0: "auto", 1: "plane", 2: "split"}
+VARIANTS = {0: "auto", 1: "plane", 2: "split", 3: "bucketed"}
 
 
 def stream_ptr(device=None):
@@ -27,7 +27,7 @@ class Plan:
     """``msf_plan`` plus its workspace on ``device``."""
 
     def __init__(self, dims, box, batch=0, variant=0, tile_w=0, rows_per_block=0,
-                 deposit_block=0, device=None):
+                 deposit_block=0, max_atoms=0, device=None):
         lib = load()
         if not torch.cuda.is_available():
             raise RuntimeError("mdsf needs a CUDA device (GB300); no CPU fallback exists")
@@ -37,7 +37,8 @@ class Plan:
         self.box = tuple(float(b) for b in box)
         desc = _lib.PlanDesc(self.dims[0], self.dims[1], self.dims[2], int(batch),
                              (C.c_double * 3)(*self.box), int(variant), int(tile_w),
-                             int(rows_per_block), int(deposit_block))
+                             int(rows_per_block), int(deposit_block), int(max_atoms))
+        self.max_atoms = int(max_atoms)
         h = c_p()
         call("msf_plan_create", C.byref(h), C.byref(desc))
         self._h = h
@@ -50,6 +51,7 @@ class Plan:
         call("msf_plan_query", h, q)
         self.variant, self.tile_w, self.rows_per_block, self.batch = q[0], q[1], q[2], q[3]
         self.deposit_block, self.plane_threads, self.nh = q[4], q[5], q[7]
+        self.tma = bool(q[6])      # x pass fed by TMA tile loads
         self.workspace_bytes = nbytes
 
     @property
@@ -67,7 +69,7 @@ class Plan:
     def tuning(self):
         return dict(variant=VARIANTS[self.variant], tile_w=self.tile_w,
                     rows_per_block=self.rows_per_block, batch=self.batch,
-                    deposit_block=self.deposit_block)
+                    deposit_block=self.deposit_block, tma=self.tma)
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -40,7 +40,8 @@ def test_strerror_and_version():
 
 def _desc(dims=(64, 64, 64), box=(2.5, 2.5, 2.5), **kw):
     d = _lib.PlanDesc(*dims, kw.get("batch", 0), (C.c_double * 3)(*box), kw.get("variant", 0),
-                      kw.get("tile_w", 0), kw.get("rows_per_block", 0), kw.get("deposit_block", 0))
+                      kw.get("tile_w", 0), kw.get("rows_per_block", 0), kw.get("deposit_block", 0),
+                      kw.get("max_atoms", 0))
     return d
 
 
@@ -53,8 +54,9 @@ def create(**kw):
 
 @pytest.mark.parametrize("kw,code", [
     (dict(dims=(1, 64, 64)), -2), (dict(dims=(64, 2048, 64)), -2), (dict(box=(0.0, 1, 1)), -1),
-    (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=3), -1),
-    (dict(tile_w=12), -1), (dict(deposit_block=100), -1),
+    (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=4), -1),
+    (dict(tile_w=12), -1), (dict(deposit_block=100), -1), (dict(max_atoms=-1), -1),
+    (dict(dims=(48, 48, 48), variant=3), -2),
 ])
 def test_plan_create_rejects(kw, code):
     st, h = create(**kw)
@@ -63,14 +65,18 @@ def test_plan_create_rejects(kw, code):
 
 def test_plan_layout_and_query():
     lib = mdsf.load()
-    st, h = create(dims=(256, 256, 128), box=(16.0, 13.856, 8.0), batch=4)
+    st, h = create(dims=(256, 256, 128), box=(16.0, 13.856, 8.0), batch=4, max_atoms=200_000)
     assert st == 0
     ws = lib.msf_plan_workspace_bytes(h)
     V, Vh = 256 * 256 * 128, 256 * 256 * 65
-    assert ws >= 4 * (4 * V + 8 * Vh)
+    assert ws >= 4 * (8 * Vh + 8 * 200_000)       # spectra + atom buckets, no density grids
+    assert ws < 4 * (4 * V + 8 * Vh)
     q = (C.c_int32 * 8)()
     assert lib.msf_plan_query(h, q) == 0
-    assert q[0] == 1 and q[3] == 4 and q[7] == 65   # fused plane variant, batch 4, nh
+    assert q[0] == 3 and q[3] == 4 and q[7] == 65   # bucketed variant, batch 4, nh
+    st1, h1 = create(dims=(256, 256, 128), box=(16.0, 13.856, 8.0), batch=4, variant=1)
+    assert st1 == 0 and lib.msf_plan_workspace_bytes(h1) >= 4 * (4 * V + 8 * Vh)
+    lib.msf_plan_destroy(h1)
     # an unbound plan refuses work before touching the GPU
     assert lib.msf_hist_sf_f32(h, C.c_void_p(16), 10, 1, None, 0, C.c_void_p(16), None) == -6
     assert lib.msf_power_accum_i32(h, C.c_void_p(16), 1, C.c_void_p(16), None) == -6

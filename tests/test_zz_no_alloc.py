@@ -19,7 +19,7 @@ TOL = 1e-5   # the S(q) tolerance used by every chain test
 
 
 def _ref_sf(p4, box, dims):
-    plan = mdsf.get_plan(dims, box)
+    plan = mdsf.get_plan(dims, box, max_atoms=p4.shape[1])
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device="cuda")
     lib = mdsf.load()
     st = lib.msf_hist_sf_f32(plan.handle, c_p(p4.data_ptr()), p4.shape[1], p4.shape[0], None, 0,
