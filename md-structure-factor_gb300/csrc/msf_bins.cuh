@@ -33,22 +33,39 @@ struct DepArgs {
   int64_t V;
 };
 
+// The estimate floor(x*n/L) is off by at most one bin; both neighbouring
+// edges are loaded together (one dependent round trip) and the rare
+// misestimate is corrected by the loops.
 __device__ __forceinline__ int bin_f32(float x, int n, float inv, const float* __restrict__ flo,
                                        const float* __restrict__ fhi) {
-  if (!(x >= __ldg(flo)) || !(x <= __ldg(fhi + n))) return -1;  // also drops NaN
+  const float lo_edge = __ldg(flo), hi_edge = __ldg(fhi + n);
   int b = (int)(x * inv);
   b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
-  while (b > 0 && x < __ldg(flo + b)) --b;
-  while (b < n - 1 && x >= __ldg(flo + b + 1)) ++b;
+  const float e0 = __ldg(flo + b), e1 = __ldg(flo + b + 1);
+  if (!(x >= lo_edge) || !(x <= hi_edge)) return -1;  // also drops NaN
+  if (x < e0) {
+    --b;
+    while (b > 0 && x < __ldg(flo + b)) --b;
+  } else if (b < n - 1 && x >= e1) {
+    ++b;
+    while (b < n - 1 && x >= __ldg(flo + b + 1)) ++b;
+  }
   return b;
 }
 
 __device__ __forceinline__ int bin_f64(double x, int n, float inv, const double* __restrict__ e) {
-  if (!(x >= __ldg(e)) || !(x <= __ldg(e + n))) return -1;
+  const double lo_edge = __ldg(e), hi_edge = __ldg(e + n);
   int b = (int)((float)x * inv);
   b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
-  while (b > 0 && x < __ldg(e + b)) --b;
-  while (b < n - 1 && x >= __ldg(e + b + 1)) ++b;
+  const double e0 = __ldg(e + b), e1 = __ldg(e + b + 1);
+  if (!(x >= lo_edge) || !(x <= hi_edge)) return -1;
+  if (x < e0) {
+    --b;
+    while (b > 0 && x < __ldg(e + b)) --b;
+  } else if (b < n - 1 && x >= e1) {
+    ++b;
+    while (b < n - 1 && x >= __ldg(e + b + 1)) ++b;
+  }
   return b;
 }
 

@@ -1,121 +1,58 @@
 // msf_fused.cu -- the bucketed histogram + FFT chain for power-of-two grids.
 //
 // Per batch of frames (dens.py:277-318 in histogram form):
-//   k_bucket_count   bins of every atom (exact numpy.histogramdd search),
-//                    per-x-plane atom counts (shared-memory histogram, one
-//                    global atomic per non-empty plane per block)
-//   k_bucket_scan    exclusive scan of the counts -> plane offsets
-//   k_bucket_fill    bins again; each atom appends (y*n2 + z, w) to its
-//                    plane's bucket, lanes of a warp that share a plane
-//                    taking one atomicAdd on the cursor (__match_any_sync)
-//   k_plane_ct       one CTA per (frame, x): the plane's atoms are added into
-//                    an int32 plane in shared memory (integer atomics, so the
-//                    grid is exact and independent of order), placed at the
-//                    digit-reversed positions of both FFT axes; then a DIT
-//                    z-FFT of row pairs y = 2p, 2p+1 packed as x[2p] + i x[2p+1],
-//                    a DIT half-length y-FFT over p, and the 2-D real split
+//   k_bucket_sort    every block bins its 4096 atoms (exact numpy.histogramdd
+//                    search), counting-sorts them by x-plane in shared memory
+//                    (lanes of a warp that share a plane merged with
+//                    __match_any_sync) and writes (y*n2 + z, w) entries plus the
+//                    plane offsets of its segment
+//   k_plane_ct       one CTA per (frame, x): the plane's atoms, gathered from
+//                    every segment, are added into the plane in shared memory
+//                    (FP32 atomics on integer weights: exact and independent
+//                    of order); then a two-pass register z-FFT of row pairs
+//                    y = 2p, 2p+1 packed as x[2p] + i x[2p+1], a two-pass
+//                    half-length y-FFT over p, and the 2-D real split
 //                      E = (W[q,k] + conj W[-q,-k])/2, O = (W[q,k] - conj W[-q,-k])/(2i)
 //                      Y[q,k] = E + w^q O, Y[q+P,k] = E - w^q O   (w = e^{-2 pi i/n1})
 //                    written as the (n1, n2/2+1) half plane.  The density grid
 //                    never goes to global memory.
-//   k_xpower_ct      x-FFT of W spectrum columns for every frame of the batch,
-//                    |F|^2 summed over the batch in FP32, one FP64 RMW of sf.
-// All FFT lengths are template constants (msf_ct.cuh).
+//   k_xpower_tma     (msf_xtma.cu; k_xpower_ct without TMA) x-FFT of W spectrum
+//                    columns for every frame of the batch, |F|^2 summed over
+//                    the batch in FP32, one FP64 RMW of sf.
+// All FFT lengths are template constants (msf_r2.cuh, msf_ct.cuh).
 #include "msf_bins.cuh"
 #include "msf_ct.cuh"
+#include "msf_r2.cuh"
 
 namespace msf {
 
 // ------------------------------------------------------------- bucketing
+// One kernel: every block takes kBucketAtoms consecutive atoms of one frame,
+// bins them (exact numpy.histogramdd search), counting-sorts them by x-plane
+// in shared memory and writes them to its own segment of the bucket array,
+// plus the (n0 + 1) plane offsets of that segment.  No global atomics and no
+// global scan: the plane kernel gathers plane x from every block's segment.
 struct BucketArgs {
   DepArgs d;
-  int* counts;      // (batch, n0)
-  int* offsets;     // (batch, n0 + 1)
-  int* cursor;      // (batch, n0)
-  int2* bucket;     // (batch, max_atoms)
-  int64_t bucket_stride;
+  int* boff;        // (batch, nblk, n0 + 1) per-block plane offsets
+  int2* bucket;     // (batch, nblk * kBucketAtoms) entries (y*n2 + z, w)
+  int nblk;
 };
 
-// Each block owns kBucketIter * 256 consecutive atoms of one frame and talks
-// to the global per-plane counters once per plane (not once per atom), so the
-// n0 counters see ~n_atoms / 4096 atomics each whatever the atom order.
 constexpr int kBucketThreads = 256;
-constexpr int kBucketIter = 16;
-constexpr int kBucketAtoms = kBucketThreads * kBucketIter;
+constexpr int kBucketIter = kBucketAtoms / kBucketThreads;
 
 template <int MODE>
-__global__ void __launch_bounds__(kBucketThreads) k_bucket_count(BucketArgs a) {
-  __shared__ int hist[kMaxN];
+__global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
+  __shared__ int hist[kMaxN + 1];
+  __shared__ int warp_sum[kBucketThreads / 32];
   const int frame = blockIdx.y;
+  const int blk = blockIdx.x;
   const int n0 = a.d.n0;
-  for (int i = threadIdx.x; i < n0; i += kBucketThreads) hist[i] = 0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i <= n0; i += kBucketThreads) hist[i] = 0;
   __syncthreads();
-  const int64_t a0 = (int64_t)blockIdx.x * kBucketAtoms + threadIdx.x;
-#pragma unroll 4
-  for (int it = 0; it < kBucketIter; ++it) {
-    const int64_t i = a0 + it * kBucketThreads;
-    int b0 = -1, b1, b2, w;
-    if (i < a.d.n_atoms && atom_bins<MODE>(a.d, frame, i, b0, b1, b2, w)) atomicAdd(&hist[b0], 1);
-  }
-  __syncthreads();
-  int* c = a.counts + (int64_t)frame * n0;
-  for (int k = threadIdx.x; k < n0; k += kBucketThreads)
-    if (hist[k]) atomicAdd(c + k, hist[k]);
-}
-
-// one block per frame; n0 <= kMaxN
-__global__ void __launch_bounds__(1024) k_bucket_scan(BucketArgs a) {
-  __shared__ int sh[kMaxN];
-  __shared__ int warp_tot[32];
-  const int frame = blockIdx.x;
-  const int n0 = a.d.n0;
-  int* c = a.counts + (int64_t)frame * n0;
-  int* off = a.offsets + (int64_t)frame * (n0 + 1);
-  int* cur = a.cursor + (int64_t)frame * n0;
-  const int t = threadIdx.x;
-  const int v = t < n0 ? c[t] : 0;
-  // inclusive warp scan
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if ((t & 31) >= o) x += y;
-  }
-  if ((t & 31) == 31) warp_tot[t >> 5] = x;
-  __syncthreads();
-  if (t < 32) {
-    int w = (t < (int)(blockDim.x >> 5)) ? warp_tot[t] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, w, o);
-      if (t >= o) w += y;
-    }
-    warp_tot[t] = w;
-  }
-  __syncthreads();
-  const int incl = x + ((t >> 5) ? warp_tot[(t >> 5) - 1] : 0);
-  if (t < n0) {
-    sh[t] = incl - v;
-    off[t] = incl - v;
-    cur[t] = incl - v;
-    c[t] = 0;              // counts ready for the next batch
-  }
-  if (t == n0 - 1) off[n0] = incl;
-}
-
-// Same atoms per block as k_bucket_count: count the block's atoms per plane
-// in shared memory, reserve one contiguous range per plane with a single
-// global atomic, then place every atom with a shared-memory atomic.  Lanes of
-// a warp that share a plane are first merged with __match_any_sync.
-template <int MODE>
-__global__ void __launch_bounds__(kBucketThreads) k_bucket_fill(BucketArgs a) {
-  __shared__ int slot[kMaxN];
-  const int frame = blockIdx.y;
-  const int n0 = a.d.n0;
-  const int lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < n0; i += kBucketThreads) slot[i] = 0;
-  __syncthreads();
-  const int64_t a0 = (int64_t)blockIdx.x * kBucketAtoms + threadIdx.x;
+  const int64_t a0 = (int64_t)blk * kBucketAtoms + tid;
   int key[kBucketIter], vox[kBucketIter], wt[kBucketIter];
 #pragma unroll
   for (int it = 0; it < kBucketIter; ++it) {
@@ -125,14 +62,45 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_fill(BucketArgs a) {
     key[it] = valid ? b0 : -1;
     vox[it] = b1 * a.d.n2 + b2;
     wt[it] = w;
-    if (valid) atomicAdd(&slot[b0], 1);
+    if (valid) atomicAdd(&hist[b0], 1);
   }
   __syncthreads();
-  int* cur = a.cursor + (int64_t)frame * n0;
-  for (int k = threadIdx.x; k < n0; k += kBucketThreads)
-    if (slot[k]) slot[k] = atomicAdd(cur + k, slot[k]);
+  // exclusive scan of hist[0..n0) -> offsets (each thread owns up to 4 consecutive planes)
+  const int per = (n0 + kBucketThreads - 1) / kBucketThreads;
+  int loc[kMaxN / kBucketThreads];
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < kMaxN / kBucketThreads; ++j) {
+    const int idx = tid * per + j;
+    loc[j] = (j < per && idx < n0) ? hist[idx] : 0;
+    sum += loc[j];
+  }
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_sum[warp] = incl;
   __syncthreads();
-  int2* bk = a.bucket + frame * a.bucket_stride;
+  int before = 0;
+#pragma unroll
+  for (int w = 0; w < kBucketThreads / 32; ++w) before += (w < warp) ? warp_sum[w] : 0;
+  int run = before + incl - sum;
+  int* bo = a.boff + ((int64_t)frame * a.nblk + blk) * (n0 + 1);
+  __syncthreads();                       // every thread has read its counts
+#pragma unroll
+  for (int j = 0; j < kMaxN / kBucketThreads; ++j) {
+    const int idx = tid * per + j;
+    if (j < per && idx < n0) {
+      hist[idx] = run;                   // becomes the placement cursor
+      bo[idx] = run;
+      run += loc[j];
+    }
+  }
+  if (tid == kBucketThreads - 1) bo[n0] = before + incl;
+  __syncthreads();
+  int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
 #pragma unroll
   for (int it = 0; it < kBucketIter; ++it) {
     const bool valid = key[it] >= 0;
@@ -141,7 +109,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_fill(BucketArgs a) {
       const unsigned peers = __match_any_sync(vm, key[it]);
       const int leader = __ffs(peers) - 1;
       int base = 0;
-      if (lane == leader) base = atomicAdd(&slot[key[it]], __popc(peers));
+      if (lane == leader) base = atomicAdd(&hist[key[it]], __popc(peers));
       base = __shfl_sync(peers, base, leader);
       bk[base + __popc(peers & ((1u << lane) - 1u))] = make_int2(vox[it], wt[it]);
     }
@@ -151,9 +119,9 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_fill(BucketArgs a) {
 // ----------------------------------------------------------- plane (z, y)
 struct PlaneCtArgs {
   // bucket source
-  const int* offsets;
+  const int* boff;
   const int2* bucket;
-  int64_t bucket_stride;
+  int nblk;
   int n0;
   // grid source
   const void* grids;
@@ -173,7 +141,9 @@ struct PlaneShape {
   static constexpr int SP = P + 1;      // odd line stride: conflict-free columns
   static constexpr int NH = N2 / 2 + 1;
   static constexpr int NT = (N2 * P >= 16384) ? 1024 : ((N2 * P >= 4096) ? 512 : 256);
-  static constexpr size_t SMEM = (size_t)N2 * SP * sizeof(float2) + (size_t)(N2 + 2 * P) * sizeof(float2);
+  // plane, twiddles, then the segment tables of the bucket gather
+  static constexpr size_t SMEM = (size_t)N2 * SP * sizeof(float2) + (size_t)(N2 + 2 * P) * sizeof(float2) +
+                                 (size_t)(2 * NT + 1 + NT / 32) * sizeof(int);
 };
 
 // SRC 0: atoms from the plane's bucket; SRC 1: a dense grid (int32/float32/float64)
@@ -193,19 +163,63 @@ __global__ void __launch_bounds__(PlaneShape<N1, N2>::NT) k_plane_ct(PlaneCtArgs
   for (int i = threadIdx.x; i < N2; i += NT) twz[i] = a.twz[i];
   for (int i = threadIdx.x; i < P; i += NT) { twp[i] = a.twp[i]; twy[i] = a.twy[i]; }
   if (SRC == 0) {
-    int4* z4 = reinterpret_cast<int4*>(buf);
-    for (int i = threadIdx.x; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
-    __syncthreads();
-    const int* off = a.offsets + (int64_t)frame * (a.n0 + 1);
-    const int e0 = off[x], e1 = off[x + 1];
-    const int2* bk = a.bucket + frame * a.bucket_stride;
-    for (int e = e0 + threadIdx.x; e < e1; e += NT) {
-      const int2 v = bk[e];
-      const int y = v.x / N2, z = v.x % N2;
-      atomicAdd(bufi + 2 * (ct::pos<N2>(z) * SP + ct::pos<P>(y >> 1)) + (y & 1), v.y);
+    // The plane's atoms sit in one segment per bucketing block.  Thread t
+    // loads segment t's bounds first (the loads overlap the zeroing below);
+    // a block scan of the segment lengths then lets every thread fetch one
+    // entry of the concatenated segments in a single round of loads.
+    int* seg_start = reinterpret_cast<int*>(twy + P);   // NT + 1 ints
+    int* seg_lo = seg_start + NT + 1;                   // NT ints
+    int* warp_sum = seg_lo + NT;                        // NT / 32 ints
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool flat = a.nblk <= NT;
+    int lo = 0, cnt = 0;
+    if (flat && tid < a.nblk) {
+      const int* bo = a.boff + ((int64_t)frame * a.nblk + tid) * (a.n0 + 1);
+      lo = bo[x];
+      cnt = bo[x + 1] - lo;
     }
+    int4* z4 = reinterpret_cast<int4*>(buf);
+    for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sum[warp] = incl;
     __syncthreads();
-    for (int i = threadIdx.x; i < 2 * N2 * SP; i += NT) buff[i] = (float)bufi[i];
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_sum[w];
+    seg_start[tid] = before + incl - cnt;
+    seg_lo[tid] = lo;
+    if (tid == NT - 1) seg_start[NT] = before + incl;
+    __syncthreads();
+    // integer weights summed in FP32: exact (and order-independent) while a
+    // voxel's total stays below 2^24 electrons
+    if (flat) {
+      const int total = seg_start[NT];
+      for (int e = tid; e < total; e += NT) {
+        int s0 = 0, s1 = a.nblk - 1;     // last segment with seg_start <= e
+        while (s0 < s1) {
+          const int m = (s0 + s1 + 1) >> 1;
+          if (seg_start[m] <= e) s0 = m; else s1 = m - 1;
+        }
+        const int2 v = a.bucket[((int64_t)frame * a.nblk + s0) * kBucketAtoms + seg_lo[s0] + (e - seg_start[s0])];
+        const int y = v.x / N2, z = v.x % N2;
+        atomicAdd(buff + 2 * (z * SP + (y >> 1)) + (y & 1), (float)v.y);
+      }
+    } else {
+      for (int blk = warp; blk < a.nblk; blk += NT / 32) {
+        const int* bo = a.boff + ((int64_t)frame * a.nblk + blk) * (a.n0 + 1);
+        const int e0 = bo[x], e1 = bo[x + 1];
+        const int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
+        for (int e = e0 + lane; e < e1; e += 32) {
+          const int2 v = bk[e];
+          const int y = v.x / N2, z = v.x % N2;
+          atomicAdd(buff + 2 * (z * SP + (y >> 1)) + (y & 1), (float)v.y);
+        }
+      }
+    }
   } else {
     const int64_t g0 = frame * a.V + (int64_t)x * N1 * N2;
     for (int e = threadIdx.x; e < N1 * N2; e += NT) {
@@ -214,12 +228,12 @@ __global__ void __launch_bounds__(PlaneShape<N1, N2>::NT) k_plane_ct(PlaneCtArgs
       if (a.grid_kind == kGridI32) v = (float)__ldg(static_cast<const int32_t*>(a.grids) + g0 + e);
       else if (a.grid_kind == kGridF32) v = __ldg(static_cast<const float*>(a.grids) + g0 + e);
       else v = (float)__ldg(static_cast<const double*>(a.grids) + g0 + e);
-      buff[2 * (ct::pos<N2>(z) * SP + ct::pos<P>(y >> 1)) + (y & 1)] = v;
+      buff[2 * (z * SP + (y >> 1)) + (y & 1)] = v;
     }
   }
   __syncthreads();
-  ct::dit<N2, P, SP, 1, NT, true>(buf, twz);    // z: lines = pairs p, elements stride SP
-  ct::dit<P, N2, 1, SP, NT, true>(buf, twp);    // half y: lines = kz, elements stride 1
+  r2::fft2_lines<N2, P, SP, 1, NT>(buf, twz);    // z: lines = pairs p, samples stride SP
+  r2::fft2_lines<P, N2, 1, SP, NT>(buf, twp);    // half y: lines = kz, samples stride 1
   float2* out = a.C + frame * a.Vh + (int64_t)x * N1 * NH;
   for (int e = threadIdx.x; e < P * NH; e += NT) {
     const int q = e / NH, k = e % NH;
@@ -372,11 +386,9 @@ size_t ct_plane_smem(int n1, int n2) {
 static BucketArgs bucket_args(const msf_plan* p) {
   BucketArgs b;
   b.d = dep_args(p);
-  b.counts = ws_ptr<int>(p, p->off_counts);
-  b.offsets = ws_ptr<int>(p, p->off_offsets);
-  b.cursor = ws_ptr<int>(p, p->off_cursor);
+  b.boff = ws_ptr<int>(p, p->off_offsets);
   b.bucket = ws_ptr<int2>(p, p->off_bucket);
-  b.bucket_stride = p->max_atoms;
+  b.nblk = (int)((p->max_atoms + kBucketAtoms - 1) / kBucketAtoms);
   return b;
 }
 
@@ -391,40 +403,32 @@ int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weight
   b.d.frame_stride = frame_stride;
   b.d.scale = scale;
   b.d.flags = flags;
-  const int64_t nb = (n_atoms + kBucketAtoms - 1) / kBucketAtoms;
-  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
-  if (nb > 0) {
-    dim3 grid((unsigned)nb, nframes);
-    switch (deposit_mode(layout, scale || (flags & MSF_WRAP))) {
-      case 0: k_bucket_count<0><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 1: k_bucket_count<1><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 2: k_bucket_count<2><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 3: k_bucket_count<3><<<grid, kBucketThreads, 0, st>>>(b); break;
-      default: k_bucket_count<4><<<grid, kBucketThreads, 0, st>>>(b); break;
-    }
-  }
-  k_bucket_scan<<<nframes, 1024, 0, st>>>(b);
-  if (nb > 0) {
-    dim3 grid((unsigned)nb, nframes);
-    switch (deposit_mode(layout, scale || (flags & MSF_WRAP))) {
-      case 0: k_bucket_fill<0><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 1: k_bucket_fill<1><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 2: k_bucket_fill<2><<<grid, kBucketThreads, 0, st>>>(b); break;
-      case 3: k_bucket_fill<3><<<grid, kBucketThreads, 0, st>>>(b); break;
-      default: k_bucket_fill<4><<<grid, kBucketThreads, 0, st>>>(b); break;
-    }
+  if (b.nblk < 1) b.nblk = 1;
+  // every block of the plan's capacity runs, so blocks past n_atoms publish
+  // empty segments and the plane kernel never reads stale offsets
+  dim3 grid((unsigned)b.nblk, nframes);
+  switch (deposit_mode(layout, scale || (flags & MSF_WRAP))) {
+    case 0: k_bucket_sort<0><<<grid, kBucketThreads, 0, st>>>(b); break;
+    case 1: k_bucket_sort<1><<<grid, kBucketThreads, 0, st>>>(b); break;
+    case 2: k_bucket_sort<2><<<grid, kBucketThreads, 0, st>>>(b); break;
+    case 3: k_bucket_sort<3><<<grid, kBucketThreads, 0, st>>>(b); break;
+    default: k_bucket_sort<4><<<grid, kBucketThreads, 0, st>>>(b); break;
   }
   return launch_status();
 }
 
 // The bucketed atoms of one frame added into a dense int32 grid (one CTA per
 // x-plane): what k_plane_ct deposits in shared memory, made visible.
-__global__ void __launch_bounds__(256) k_bucket_to_grid(const int* offsets, const int2* bucket, int n0,
-                                                        int64_t plane, int32_t* grid) {
+__global__ void __launch_bounds__(256) k_bucket_to_grid(BucketArgs a, int64_t plane, int32_t* grid) {
   const int x = blockIdx.x;
-  for (int e = offsets[x] + threadIdx.x; e < offsets[x + 1]; e += blockDim.x) {
-    const int2 v = bucket[e];
-    atomicAdd(grid + x * plane + v.x, v.y);
+  const int n0 = a.d.n0;
+  for (int blk = 0; blk < a.nblk; ++blk) {
+    const int* bo = a.boff + (int64_t)blk * (n0 + 1);
+    const int2* bk = a.bucket + (int64_t)blk * kBucketAtoms;
+    for (int e = bo[x] + threadIdx.x; e < bo[x + 1]; e += blockDim.x) {
+      const int2 v = bk[e];
+      atomicAdd(grid + x * plane + v.x, v.y);
+    }
   }
 }
 
@@ -433,17 +437,19 @@ int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int 
   const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
   int s = fused_bucket_batch(p, pos, weights, layout, n_atoms, 1, fstride, scale, flags, st);
   if (s) return s;
-  k_bucket_to_grid<<<p->n0, 256, 0, st>>>(ws_ptr<int>(p, p->off_offsets), ws_ptr<int2>(p, p->off_bucket),
-                                           p->n0, (int64_t)p->n1 * p->n2, grid);
+  BucketArgs b = bucket_args(p);
+  if (b.nblk < 1) b.nblk = 1;
+  k_bucket_to_grid<<<p->n0, 256, 0, st>>>(b, (int64_t)p->n1 * p->n2, grid);
   return launch_status();
 }
 
 static PlaneCtArgs plane_args(const msf_plan* p) {
   PlaneCtArgs a;
   memset(&a, 0, sizeof(a));
-  a.offsets = ws_ptr<int>(p, p->off_offsets);
+  a.boff = ws_ptr<int>(p, p->off_offsets);
   a.bucket = ws_ptr<int2>(p, p->off_bucket);
-  a.bucket_stride = p->max_atoms;
+  a.nblk = (int)((p->max_atoms + kBucketAtoms - 1) / kBucketAtoms);
+  if (a.nblk < 1) a.nblk = 1;
   a.n0 = p->n0;
   a.V = grid_elems(p);
   a.C = ws_ptr<float2>(p, p->off_cplx);

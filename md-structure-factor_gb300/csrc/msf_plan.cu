@@ -201,10 +201,12 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   p->off_edges_fhi = o; o = align_up(o + ne * sizeof(float));
   // density grids: the bucketed variant never materialises them
   p->off_grid = o; o = align_up(o + (variant == 3 ? 0 : (size_t)p->batch * grid_elems(p) * sizeof(int32_t)));
-  p->off_counts = o; o = align_up(o + (size_t)p->batch * n[0] * sizeof(int));
-  p->off_offsets = o; o = align_up(o + (size_t)p->batch * (n[0] + 1) * sizeof(int));
-  p->off_cursor = o; o = align_up(o + (size_t)p->batch * n[0] * sizeof(int));
-  p->off_bucket = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * p->max_atoms * 8 : 0));
+  // per-block plane offsets and atom entries of the bucketed variant
+  const int64_t nblk = variant == 3 ? (p->max_atoms + kBucketAtoms - 1) / kBucketAtoms : 0;
+  p->off_counts = o;
+  p->off_offsets = o; o = align_up(o + (size_t)p->batch * (nblk > 0 ? nblk : 1) * (n[0] + 1) * sizeof(int));
+  p->off_cursor = o;
+  p->off_bucket = o; o = align_up(o + (size_t)p->batch * nblk * kBucketAtoms * 8);
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
   p->ws_bytes = o;
   return MSF_OK;
@@ -249,8 +251,6 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
                                     (size_t)p->batch * grid_elems(p) * sizeof(int32_t), st));
     if (s) return s;
   }
-  s = cuda_status(cudaMemsetAsync(p->ws + p->off_counts, 0, (size_t)p->batch * p->n0 * sizeof(int), st));
-  if (s) return s;
   s = xtma_prepare(p);
   if (s) return s;
   p->bound = 1;

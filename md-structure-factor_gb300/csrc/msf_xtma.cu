@@ -9,9 +9,9 @@
 // over the frames of the tile in FP32, one FP64 read-modify-write of sf per
 // tile.  Waits are bounded: on timeout the kernel latches MSF_E_TIMEOUT in
 // the plan status word and returns.
-#include <cuda.h>
-
 #include "msf_ct.cuh"
+#include "msf_r2.cuh"
+#include "msf_tma.cuh"
 
 namespace msf {
 
@@ -24,41 +24,6 @@ struct XTmaArgs {
   int* status;
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-// true when the phase with the given parity has completed
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-      : "memory");
-}
-
-constexpr long long kWaitLimit = 1LL << 26;  // try_wait polls before giving up (seconds)
-
 template <int N0, int W>
 struct XTmaShape {
   static constexpr int NT = 256;
@@ -70,7 +35,8 @@ struct XTmaShape {
 };
 
 template <int N0, int W>
-__global__ void __launch_bounds__(256) k_xpower_tma(const __grid_constant__ CUtensorMap map, XTmaArgs a) {
+__global__ void __launch_bounds__(256, (N0 <= 256 ? 3 : 1)) k_xpower_tma(const __grid_constant__ CUtensorMap map,
+                                                                       XTmaArgs a) {
   using S = XTmaShape<N0, W>;
   constexpr int NT = S::NT, EPT = S::EPT;
   static_assert(EPT * NT == N0 * W, "tile must split evenly over the threads");
@@ -110,15 +76,15 @@ __global__ void __launch_bounds__(256) k_xpower_tma(const __grid_constant__ CUte
     if (total > 1) issue(1);
   }
   uint32_t phase0 = 0, phase1 = 0;
-  int pos_x[EPT];
+  // pass-2 items (k1, column) owned by this thread; X[k1 + B*k2] power in acc
+  constexpr int A = r2::Split2<N0>::A, B = r2::Split2<N0>::B;
+  constexpr int ITEMS2 = B * W;
+  constexpr int PER = (ITEMS2 + NT - 1) / NT;
+  float acc[PER][A];
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const int e = tid + i * NT;
-    pos_x[i] = ct::pos<N0>(e / W) * W + (e % W);
-  }
-  float acc[EPT];
+  for (int j = 0; j < PER; ++j)
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) acc[i] = 0.f;
+    for (int k = 0; k < A; ++k) acc[j][k] = 0.f;
 
   for (int s = 0; s < total; ++s) {
     const int b = s & 1;
@@ -135,25 +101,41 @@ __global__ void __launch_bounds__(256) k_xpower_tma(const __grid_constant__ CUte
     }
     if (b) phase1 ^= 1u; else phase0 ^= 1u;
     float2* t = b ? buf1 : buf0;
-    ct::dif<N0, W, W, 1, NT, true>(t, tw);
+    r2::pass1<N0, W, W, 1, NT>(t, tw);
+    __syncthreads();
 #pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const float2 v = t[pos_x[i]];
-      acc[i] = fmaf(v.x, v.x, fmaf(v.y, v.y, acc[i]));
+    for (int j = 0; j < PER; ++j) {
+      const int it = j * NT + tid;
+      if (ITEMS2 % NT == 0 || it < ITEMS2) {
+        const int l = it % W, k1 = it / W;
+        const float2* p = t + l + A * k1 * W;
+        float2 r[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) r[n1] = p[n1 * W];
+        reg::reg_dft<A>(r);
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = fmaf(r[k2].x, r[k2].x, fmaf(r[k2].y, r[k2].y, acc[j][k2]));
+      }
     }
     const int frame = s % a.nframes;
     if (frame == a.nframes - 1) {
       const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
       const int64_t f0 = (int64_t)tile * W;
 #pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int e = tid + i * NT;
-        const int x = e / W, w = e % W;
-        if (f0 + w < a.F) {
-          double* d = a.sf + (int64_t)x * a.F + f0 + w;
-          *d = *d + (double)acc[i];
+      for (int j = 0; j < PER; ++j) {
+        const int it = j * NT + tid;
+        const int l = it % W, k1 = it / W;
+        const bool ok = (ITEMS2 % NT == 0 || it < ITEMS2) && f0 + l < a.F;
+        double* d = a.sf + (int64_t)k1 * a.F + f0 + l;
+        // all loads of the column first (independent), then the adds and stores
+        double old[A];
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) old[k2] = ok ? __ldcg(d + (int64_t)B * k2 * a.F) : 0.0;
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) {
+          if (ok) __stcg(d + (int64_t)B * k2 * a.F, old[k2] + (double)acc[j][k2]);
+          acc[j][k2] = 0.f;
         }
-        acc[i] = 0.f;
       }
     }
     __syncthreads();   // every thread is done with buffer b
