@@ -217,7 +217,7 @@ def main():
         tuning["tile_w"] = args.tile_w
     if not tuning:
         from mdsf import tune
-        tuning = tune.lookup(DIMS) or {"batch": 8}
+        tuning = tune.lookup(DIMS) or {"batch": 16}
     plan = mdsf.get_plan(DIMS, box, device=dev, max_atoms=N_ATOMS, **tuning)
     st = torch.cuda.current_stream(dev)
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=dev)

@@ -100,20 +100,15 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
   }
   if (tid == kBucketThreads - 1) bo[n0] = before + incl;
   __syncthreads();
+  // placement: one independent shared-memory atomic per atom, so the
+  // iterations of a thread overlap instead of forming a chain
   int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
+  int slot[kBucketIter];
 #pragma unroll
-  for (int it = 0; it < kBucketIter; ++it) {
-    const bool valid = key[it] >= 0;
-    const unsigned vm = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      const unsigned peers = __match_any_sync(vm, key[it]);
-      const int leader = __ffs(peers) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(&hist[key[it]], __popc(peers));
-      base = __shfl_sync(peers, base, leader);
-      bk[base + __popc(peers & ((1u << lane) - 1u))] = make_int2(vox[it], wt[it]);
-    }
-  }
+  for (int it = 0; it < kBucketIter; ++it) slot[it] = key[it] >= 0 ? atomicAdd(&hist[key[it]], 1) : -1;
+#pragma unroll
+  for (int it = 0; it < kBucketIter; ++it)
+    if (slot[it] >= 0) bk[slot[it]] = make_int2(vox[it], wt[it]);
 }
 
 // ----------------------------------------------------------- plane (z, y)

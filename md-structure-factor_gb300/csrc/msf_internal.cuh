@@ -15,7 +15,7 @@ namespace msf {
 constexpr int kMaxStages = 12;
 constexpr int kMaxN = 1024;      // largest supported axis length
 constexpr int kStatusWords = 16; // device status block (int32)
-constexpr int kBucketAtoms = 4096; // atoms per bucketing block (bucketed variant)
+constexpr int kBucketAtoms = 2048; // atoms per bucketing block (bucketed variant)
 
 // Device status words (latched by kernels, read by msf_plan_status).
 enum StatusWord { kStatErr = 0, kStatBadAtom = 1, kStatBadIndex = 2 };

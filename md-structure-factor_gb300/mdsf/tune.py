@@ -52,7 +52,7 @@ def candidates(dims):
     variants = [1, 2] if n1 % 2 == 0 else [2]
     tiles = [w for w in (4, 8, 16, 32) if max(n0, n1) * w <= 4096]
     rows = sorted({max(2, min(32, 2048 // n2)), max(2, min(32, 1024 // n2)), max(2, min(32, 4096 // n2))})
-    batches = [1, 2, 4, 8]
+    batches = [2, 4, 8, 16, 32]
     for v, w, b in itertools.product(variants, tiles, batches):
         for g in (rows if v == 2 else rows[:1]):
             yield dict(variant=v, tile_w=w, rows_per_block=g, batch=b)
