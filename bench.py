@@ -181,6 +181,7 @@ def main():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--tile-w", type=int, default=0)
+    ap.add_argument("--no-overlap", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
@@ -215,6 +216,8 @@ def main():
         tuning["variant"] = args.variant
     if args.tile_w:
         tuning["tile_w"] = args.tile_w
+    if args.no_overlap:
+        tuning["options"] = 1
     if not tuning:
         from mdsf import tune
         tuning = tune.lookup(DIMS) or {"batch": 16}
@@ -442,6 +445,28 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     out["grad_evals_per_s"] = S_ / (ms / 1000.0)
     out["grad_note"] = f"systems/s: forward+adjoint of {S_} systems x {N} atoms x {M} q per launch pair"
     out["direct_pairs_per_s"] = pairs / (ms / 1000.0)
+    del r, f, q, target
+
+    # batched uneven systems: 64 systems, log-uniform 5k-300k atoms, boxes 3-16 nm,
+    # 2^a 3^b 5^c grids in 48-256, 20-200 frames, one CUDA graph over 8 streams
+    from mdsf.batch import BatchedSystems, random_batch
+    systems = random_batch(64, seed=5, device=dev)
+    frames = sum(int(s["pos_w"].shape[0]) for s in systems)
+    b = BatchedSystems(systems, n_streams=8, device=dev)
+    b.run()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(2):
+        b.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    out["batched_systems_frames_per_s"] = frames / (ms / 1000.0)
+    out["batched_systems_note"] = (f"64 systems, {frames} frames, one graph launch per run "
+                                   f"({sum(1 for i in range(64) if b.tuning(i)['variant'] == 3)} on the bucketed "
+                                   "power-of-two path)")
+    del b, systems
+    torch.cuda.empty_cache()
     return out
 
 

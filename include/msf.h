@@ -74,7 +74,15 @@ typedef struct msf_plan_desc {
   int32_t deposit_block;  /* threads per deposit block: 0 auto */
   int64_t max_atoms;      /* atoms per frame the chain may be called with (sizes the per-plane
                              atom buckets of variant 3); 0 = no buckets */
+  int32_t options;        /* MSF_PLAN_NO_OVERLAP: keep variant 3 on the caller's stream only */
 } msf_plan_desc;
+
+/* msf_plan_desc.options.  By default a variant-3 plan double-buffers its
+ * spectra and msf_plan_bind creates one internal stream and four events:
+ * the x pass of each batch then runs on that stream, overlapped with the
+ * plane FFT of the next batch (forked from and joined back to the caller's
+ * stream, so the calls stay stream-ordered and graph-capturable). */
+enum { MSF_PLAN_NO_OVERLAP = 1 };
 
 int msf_plan_create(msf_plan** plan, const msf_plan_desc* desc);
 int msf_plan_destroy(msf_plan* plan);
@@ -213,6 +221,38 @@ int msf_direct_fwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
 int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q, int32_t n_sys,
                    int32_t q_shared, const float* g, const void* AB, void* grad,
                    msf_stream_t stream);
+
+/* ----------------------------------------- batched systems (CUDA graph)
+ * Many independent systems -- each with its own atom count, frame count,
+ * box and grid shape -- through the histogram chain of msf_hist_sf_f32 in
+ * one CUDA graph.  Replaces calling dens.compute_sf (dens.py:166) once per
+ * trajectory.  msf_batch_create plans every system (host only);
+ * msf_batch_bind lays their workspaces out in one caller buffer of
+ * msf_batch_workspace_bytes(), binds the plans and captures all chains into
+ * a graph (spread over n_streams capture streams, largest systems first);
+ * msf_batch_run launches it (sf += for every system).  The graph keeps the
+ * device pointers given at creation: refresh positions in place between runs.
+ * bind synchronises `stream` once (not a hot call).
+ */
+typedef struct msf_batch msf_batch;
+typedef struct msf_batch_system {
+  const void* pos_w;       /* device float4 (n_frames, n_atoms): x, y, z, electrons */
+  const double* scale;     /* NULL or device (n_frames, 3) per-frame rescale factors */
+  double* sf;              /* device FP64 (n0, n1, n2/2+1), accumulated */
+  int64_t n_atoms, n_frames;
+  double box[3];
+  int32_t n0, n1, n2;
+  int32_t flags;           /* MSF_WRAP or 0 */
+  int32_t batch, variant, tile_w;   /* per-system tuning, 0 = default */
+} msf_batch_system;
+
+int msf_batch_create(msf_batch** batch, const msf_batch_system* systems, int32_t n_systems,
+                     int32_t n_streams);
+size_t msf_batch_workspace_bytes(const msf_batch* batch);
+int msf_batch_bind(msf_batch* batch, void* workspace, size_t workspace_bytes, msf_stream_t stream);
+int msf_batch_run(msf_batch* batch, msf_stream_t stream);
+int msf_batch_query(const msf_batch* batch, int32_t index, int32_t out[8]);
+int msf_batch_destroy(msf_batch* batch);
 
 /* ------------------------------------------- allocation-free chain variant
  * No counterpart in the reference: an addition of this library for callers

@@ -135,15 +135,17 @@ struct PlaneShape {
   static constexpr int P = N1 / 2;
   static constexpr int SP = P + 1;      // odd line stride: conflict-free columns
   static constexpr int NH = N2 / 2 + 1;
-  static constexpr int NT = (N2 * P >= 16384) ? 1024 : ((N2 * P >= 4096) ? 512 : 256);
+  static constexpr int NT = (N2 * P >= 4096) ? 512 : 256;
   // plane, twiddles, then the segment tables of the bucket gather
   static constexpr size_t SMEM = (size_t)N2 * SP * sizeof(float2) + (size_t)(N2 + 2 * P) * sizeof(float2) +
                                  (size_t)(2 * NT + 1 + NT / 32) * sizeof(int);
 };
 
 // SRC 0: atoms from the plane's bucket; SRC 1: a dense grid (int32/float32/float64)
+// Registers capped so that one x-pass CTA fits on the SM beside a plane CTA
+// (the two kernels overlap on different streams).
 template <int N1, int N2, int SRC>
-__global__ void __launch_bounds__(PlaneShape<N1, N2>::NT) k_plane_ct(PlaneCtArgs a) {
+__global__ void __maxnreg__((PlaneShape<N1, N2>::NT >= 512 ? 80 : 128)) k_plane_ct(PlaneCtArgs a) {
   using S = PlaneShape<N1, N2>;
   constexpr int P = S::P, SP = S::SP, NH = S::NH, NT = S::NT;
   extern __shared__ float2 smem[];
@@ -455,17 +457,19 @@ static PlaneCtArgs plane_args(const msf_plan* p) {
   return a;
 }
 
-int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st) {
+int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st,
+                      int buf) {
   PlaneCtArgs a = plane_args(p);
+  if (buf) a.C = ws_ptr<float2>(p, p->off_cplx2);
   a.grids = grids;
   a.grid_kind = grid_kind;
   return plane_ct(a, p->n1, p->n2, grids ? 1 : 0, p->n0, nframes, st);
 }
 
-int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
-  if (p->xtma_ready) return xtma_batch(p, nframes, sf, st);
+int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf) {
+  if (p->xtma_ready) return xtma_batch(p, nframes, sf, st, buf);
   XCtArgs a;
-  a.C = ws_ptr<float2>(p, p->off_cplx);
+  a.C = ws_ptr<float2>(p, buf ? p->off_cplx2 : p->off_cplx);
   a.Vh = half_elems(p);
   a.nframes = nframes;
   a.sf = sf;

@@ -157,6 +157,30 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
   const size_t esize = layout == kLayoutF32x4 ? 4 * sizeof(float)
                        : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
   if (p->variant == 3 && n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
+  if (p->variant == 3 && p->overlap && n_frames > p->batch) {
+    // batch b: bucket sort + plane FFT into spectrum buffer b%2 on `st`, the
+    // x pass of batch b on `side` (after that plane FFT), overlapping the
+    // plane FFT of batch b+1; the plane FFT of batch b+2 waits for the x pass
+    // of batch b before reusing its buffer; `st` finally joins `side`.
+    int s = MSF_OK;
+    int64_t k = 0;
+    for (int64_t f = 0; f < n_frames && !s; f += p->batch, ++k) {
+      const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
+      const int buf = (int)(k & 1);
+      const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;
+      s = fused_bucket_batch(p, fp, weights, layout, n_atoms, nb, fstride, scale ? scale + 3 * f : nullptr,
+                             flags, st);
+      if (!s && k >= 2) s = cuda_status(cudaStreamWaitEvent(st, p->ev_x[buf], 0));
+      if (!s) s = fused_plane_batch(p, nullptr, kGridI32, nb, st, buf);
+      if (!s) s = cuda_status(cudaEventRecord(p->ev_plane[buf], st));
+      if (!s) s = cuda_status(cudaStreamWaitEvent(p->side, p->ev_plane[buf], 0));
+      if (!s) s = fused_x_batch(p, nb, sf, p->side, buf);
+      if (!s) s = cuda_status(cudaEventRecord(p->ev_x[buf], p->side));
+    }
+    // join: every x pass (recorded in order on `side`) precedes the last event
+    if (k >= 1 && !s) s = cuda_status(cudaStreamWaitEvent(st, p->ev_x[(k - 1) & 1], 0));
+    return s;
+  }
   for (int64_t f = 0; f < n_frames; f += p->batch) {
     const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
     const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;

@@ -58,9 +58,16 @@ struct msf_plan {
   // bucketed chain (variant 3): per-x-plane atom lists
   int64_t max_atoms;
   size_t off_counts, off_offsets, off_cursor, off_bucket;
-  // TMA tensor map over the spectra for the x pass (CUtensorMap, 128 bytes)
-  alignas(64) unsigned char xtma_map[128];
+  // TMA tensor maps over the two spectrum buffers for the x pass (CUtensorMap, 128 bytes each)
+  alignas(64) unsigned char xtma_map[2][128];
   int xtma_ready;
+  // overlap (bucketed variant): spectra double-buffered, the x pass of one
+  // batch runs on `side` while the plane FFT of the next batch runs on the
+  // caller's stream; created by msf_plan_bind, released by plan_release
+  int overlap;
+  size_t off_cplx2;
+  cudaStream_t side;
+  cudaEvent_t ev_plane[2], ev_x[2];
 };
 
 namespace msf {
@@ -270,12 +277,15 @@ size_t ct_plane_smem(int n1, int n2);
 int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
                        int64_t n_atoms, int nframes, int64_t frame_stride, const double* scale,
                        int flags, cudaStream_t st);
-int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st);
-int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
+int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st,
+                      int buf = 0);
+int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf = 0);
+// destroys the streams/events a bind created (idempotent)
+void plan_release(msf_plan* p);
 // x pass with TMA tile loads (msf_xtma.cu); prepared at bind time
 bool xtma_ok(int n0, int w);
 int xtma_prepare(msf_plan* p);
-int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf);
 int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int layout, int64_t n_atoms,
                 const double* scale, int flags, int32_t* grid, cudaStream_t st);
 

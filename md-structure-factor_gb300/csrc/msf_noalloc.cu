@@ -64,6 +64,7 @@ extern "C" int msf_hist_sf_f32_noalloc(const void* pos_w, int64_t n_atoms, int64
   d.n0 = n0; d.n1 = n1; d.n2 = n2;
   d.box[0] = box_host[0]; d.box[1] = box_host[1]; d.box[2] = box_host[2];
   d.max_atoms = n_atoms;  // per-plane atom buckets of the bucketed variant
+  d.options = MSF_PLAN_NO_OVERLAP;  // no internal stream or events: nothing is created
   int fit = 0;
   for (int b = 8; b >= 1 && !fit; b /= 2) {
     d.batch = b;

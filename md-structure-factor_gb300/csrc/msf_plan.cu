@@ -94,6 +94,17 @@ __global__ void k_init_tables(TabArgs a) {
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+void plan_release(msf_plan* p) {
+  for (int i = 0; i < 2; ++i) {
+    if (p->ev_plane[i]) cudaEventDestroy(p->ev_plane[i]);
+    if (p->ev_x[i]) cudaEventDestroy(p->ev_x[i]);
+    p->ev_plane[i] = nullptr;
+    p->ev_x[i] = nullptr;
+  }
+  if (p->side) cudaStreamDestroy(p->side);
+  p->side = nullptr;
+}
+
 }  // namespace msf
 
 using namespace msf;
@@ -140,7 +151,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
     if (!(d->box[i] > 0.0) || !isfinite(d->box[i])) return MSF_E_INVALID;
   if (d->batch < 0 || d->batch > 256) return MSF_E_INVALID;
   if (d->variant < 0 || d->variant > 3) return MSF_E_INVALID;
-  if (d->max_atoms < 0) return MSF_E_INVALID;
+  if (d->max_atoms < 0 || (d->options & ~MSF_PLAN_NO_OVERLAP)) return MSF_E_INVALID;
   if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
   memset(p, 0, sizeof(*p));
@@ -163,6 +174,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   if (variant == 1 && !plane_ok) return MSF_E_UNSUPPORTED;
   if (variant == 3 && !fused_ok) return MSF_E_UNSUPPORTED;
   p->max_atoms = d->max_atoms;
+  p->overlap = variant == 3 && !(d->options & MSF_PLAN_NO_OVERLAP);
   p->variant = variant;
   p->plane_smem = plane_smem;
   p->plane_threads = (n[2] * P >= 8192) ? 512 : 256;
@@ -208,6 +220,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   p->off_cursor = o;
   p->off_bucket = o; o = align_up(o + (size_t)p->batch * nblk * kBucketAtoms * 8);
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
+  p->off_cplx2 = o; o = align_up(o + (p->overlap ? (size_t)p->batch * half_elems(p) * sizeof(float2) : 0));
   p->ws_bytes = o;
   return MSF_OK;
 }
@@ -215,6 +228,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
 extern "C" {
 
 int msf_plan_destroy(msf_plan* p) {
+  if (p) plan_release(p);
   delete p;
   return MSF_OK;
 }
@@ -250,6 +264,13 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
     s = cuda_status(cudaMemsetAsync(p->ws + p->off_grid, 0,
                                     (size_t)p->batch * grid_elems(p) * sizeof(int32_t), st));
     if (s) return s;
+  }
+  if (p->overlap && !p->side) {
+    if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
+    for (int i = 0; i < 2; ++i) {
+      if (cudaEventCreateWithFlags(&p->ev_plane[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
+      if (cudaEventCreateWithFlags(&p->ev_x[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
+    }
   }
   s = xtma_prepare(p);
   if (s) return s;

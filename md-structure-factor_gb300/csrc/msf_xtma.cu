@@ -177,16 +177,17 @@ static EncodeTiledFn encode_fn() {
 template <int N0, int W>
 static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs& a, cudaStream_t st) {
   using S = XTmaShape<N0, W>;
-  static int grid = 0;
+  static int grid = 0, sms = 0;
   if (!grid) {
     cudaFuncSetAttribute(k_xpower_tma<N0, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-    int dev = 0, sms = 0, occ = 0;
+    int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_xpower_tma<N0, W>, S::NT, S::SMEM);
     grid = (sms > 0 ? sms : 152) * (occ > 0 ? occ : 1);
   }
-  const int g = a.ntiles < grid ? a.ntiles : grid;
+  const int cap = p->overlap ? (sms > 0 ? sms : 152) : grid;
+  const int g = a.ntiles < cap ? a.ntiles : cap;
   k_xpower_tma<N0, W><<<g, S::NT, S::SMEM, st>>>(*map, a);
   return launch_status();
 }
@@ -213,16 +214,18 @@ int xtma_prepare(msf_plan* p) {
   cuuint64_t strides[1] = {(cuuint64_t)(F * sizeof(float2))};
   cuuint32_t box[2] = {(cuuint32_t)p->tile_w, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUtensorMap* m = reinterpret_cast<CUtensorMap*>(p->xtma_map);
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, p->ws + p->off_cplx, dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return MSF_OK;   // plain loads then
+  for (int k = 0; k < (p->overlap ? 2 : 1); ++k) {
+    CUtensorMap* m = reinterpret_cast<CUtensorMap*>(p->xtma_map[k]);
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, p->ws + (k ? p->off_cplx2 : p->off_cplx), dims,
+                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return MSF_OK;   // plain loads then
+  }
   p->xtma_ready = 1;
   return MSF_OK;
 }
 
-int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf) {
   XTmaArgs a;
   a.nframes = nframes;
   a.F = (int64_t)p->n1 * p->nh;
@@ -230,7 +233,7 @@ int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
   a.sf = sf;
   a.twx = ws_ptr<float2>(p, p->off_tw[0]);
   a.status = ws_ptr<int>(p, p->off_status);
-  const CUtensorMap* map = reinterpret_cast<const CUtensorMap*>(p->xtma_map);
+  const CUtensorMap* map = reinterpret_cast<const CUtensorMap*>(p->xtma_map[buf]);
 #define X(A, B) if (p->n0 == A && p->tile_w == B) return launch_xtma<A, B>(p, map, a, st);
   MSF_XTMA_CASES(X)
 #undef X

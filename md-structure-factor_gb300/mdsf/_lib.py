@@ -40,7 +40,14 @@ class MsfError(RuntimeError):
 class PlanDesc(C.Structure):
     _fields_ = [("n0", c_int), ("n1", c_int), ("n2", c_int), ("batch", c_int),
                 ("box", c_d * 3), ("variant", c_int), ("tile_w", c_int),
-                ("rows_per_block", c_int), ("deposit_block", c_int), ("max_atoms", c_i64)]
+                ("rows_per_block", c_int), ("deposit_block", c_int), ("max_atoms", c_i64),
+                ("options", c_int)]
+
+
+class BatchSystem(C.Structure):
+    _fields_ = [("pos_w", c_p), ("scale", c_p), ("sf", c_p), ("n_atoms", c_i64), ("n_frames", c_i64),
+                ("box", c_d * 3), ("n0", c_int), ("n1", c_int), ("n2", c_int), ("flags", c_int),
+                ("batch", c_int), ("variant", c_int), ("tile_w", c_int)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/msf.h
@@ -69,6 +76,12 @@ SIGNATURES = {
     "msf_ewald": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_d, c_p, c_p, c_p, c_p]),
     "msf_direct_fwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p]),
     "msf_direct_bwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p, c_p]),
+    "msf_batch_create": (c_int, [C.POINTER(c_p), C.POINTER(BatchSystem), c_int, c_int]),
+    "msf_batch_workspace_bytes": (c_size, [c_p]),
+    "msf_batch_bind": (c_int, [c_p, c_p, c_size, c_p]),
+    "msf_batch_run": (c_int, [c_p, c_p]),
+    "msf_batch_query": (c_int, [c_p, c_int, C.POINTER(c_int)]),
+    "msf_batch_destroy": (c_int, [c_p]),
     "msf_hist_sf_f32_noalloc": (c_int, [c_p, c_i64, c_i64, c_p, c_int, c_int, c_int, c_int, c_p, c_p]),
     "msf_noalloc_scratch_bytes": (c_size, []),
 }

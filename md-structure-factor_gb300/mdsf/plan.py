@@ -27,7 +27,7 @@ class Plan:
     """``msf_plan`` plus its workspace on ``device``."""
 
     def __init__(self, dims, box, batch=0, variant=0, tile_w=0, rows_per_block=0,
-                 deposit_block=0, max_atoms=0, device=None):
+                 deposit_block=0, max_atoms=0, options=0, device=None):
         lib = load()
         if not torch.cuda.is_available():
             raise RuntimeError("mdsf needs a CUDA device (GB300); no CPU fallback exists")
@@ -37,7 +37,7 @@ class Plan:
         self.box = tuple(float(b) for b in box)
         desc = _lib.PlanDesc(self.dims[0], self.dims[1], self.dims[2], int(batch),
                              (C.c_double * 3)(*self.box), int(variant), int(tile_w),
-                             int(rows_per_block), int(deposit_block), int(max_atoms))
+                             int(rows_per_block), int(deposit_block), int(max_atoms), int(options))
         self.max_atoms = int(max_atoms)
         h = c_p()
         call("msf_plan_create", C.byref(h), C.byref(desc))

@@ -41,7 +41,7 @@ def test_strerror_and_version():
 def _desc(dims=(64, 64, 64), box=(2.5, 2.5, 2.5), **kw):
     d = _lib.PlanDesc(*dims, kw.get("batch", 0), (C.c_double * 3)(*box), kw.get("variant", 0),
                       kw.get("tile_w", 0), kw.get("rows_per_block", 0), kw.get("deposit_block", 0),
-                      kw.get("max_atoms", 0))
+                      kw.get("max_atoms", 0), kw.get("options", 0))
     return d
 
 
@@ -69,8 +69,11 @@ def test_plan_layout_and_query():
     assert st == 0
     ws = lib.msf_plan_workspace_bytes(h)
     V, Vh = 256 * 256 * 128, 256 * 256 * 65
-    assert ws >= 4 * (8 * Vh + 8 * 200_000)       # spectra + atom buckets, no density grids
-    assert ws < 4 * (4 * V + 8 * Vh)
+    assert ws >= 4 * (2 * 8 * Vh + 8 * 200_000)   # double-buffered spectra + atom buckets
+    st2, h2 = create(dims=(256, 256, 128), box=(16.0, 13.856, 8.0), batch=4, max_atoms=200_000, options=1)
+    assert st2 == 0
+    assert lib.msf_plan_workspace_bytes(h2) < 4 * (4 * V + 8 * Vh)   # no density grids, one spectrum buffer
+    lib.msf_plan_destroy(h2)
     q = (C.c_int32 * 8)()
     assert lib.msf_plan_query(h, q) == 0
     assert q[0] == 3 and q[3] == 4 and q[7] == 65   # bucketed variant, batch 4, nh
