@@ -242,7 +242,7 @@ def main():
              _ptr(ew[0]), _ptr(ew[1]), _ptr(ew[2]), sp)
 
     batches = (FRAMES + plan.batch - 1) // plan.batch
-    launches_per_step = batches * {1: 3, 2: 4, 3: 5}[plan.variant] + 2
+    launches_per_step = batches * {1: 3, 2: 4, 3: 3}[plan.variant] + 2
 
     # warm-up (also primes one-time kernel attributes before graph capture)
     for _ in range(2):
@@ -328,11 +328,11 @@ def main():
     # compulsory bytes of each stage for one launch of `B` frames
     if plan.variant == 3:
         stage_bytes = {
-            1: lambda k: 2 * 16 * N_ATOMS * k + 8 * N_ATOMS * k,   # positions read twice, bucket written
+            1: lambda k: 16 * N_ATOMS * k + 8 * N_ATOMS * k,       # positions read, bucket entries written
             2: lambda k: 8 * N_ATOMS * k + 8 * Vh * k,              # bucket read, spectrum written
             4: lambda k: 8 * Vh * k + 16 * Vh,                      # spectrum read, sf read + written
         }
-        stage_names = {1: "k_bucket_count+scan+fill", 2: "k_plane_ct", 4: "k_xpower_ct"}
+        stage_names = {1: "k_bucket_sort", 2: "k_plane_ct", 4: "k_xpower_tma" if plan.tma else "k_xpower_ct"}
     else:
         stage_bytes = {
             1: lambda k: 16 * N_ATOMS * k + 4 * V * k,             # positions read, grid written
@@ -348,12 +348,17 @@ def main():
     kfull = full[0][1]
     achieved = stage_bytes[dom](kfull) / (avg_ms / 1000.0) / 1e9
     peak, peak_kind = peaks()
+    # DRAM bytes per launch of the dominant kernel from the committed ncu
+    # capture of this workload (profiles/dram_traffic.txt), when it matches
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tj = json.load(f)
-        traffic = tj.get(stage_names[dom])
-    except Exception:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                fld = line.split()
+                if len(fld) == 4 and not line.startswith("#") and fld[0] == stage_names[dom] \
+                        and fld[1] == "x".join(map(str, DIMS)) and int(fld[2]) == kfull:
+                    traffic = int(fld[3])
+    except (OSError, ValueError):
         pass
     chain_gbs = algorithmic_bytes_per_frame() * value / world / 1e9
 
