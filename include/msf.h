@@ -205,6 +205,21 @@ int msf_ewald(const double* D, int32_t p0, int32_t p1, int32_t p2, const double*
               const double* Y, const double* Z, double K, double* xy, double* xz, double* yz,
               msf_stream_t stream);
 
+/* ------------------------------------------- cylindrical (r, z) average
+ * The ring average of plot2d.PLOT_RAD_NEW (plot2d.py:601-631), the step the
+ * reference CLI runs after compute_sf (main_gromacs.py:231 ->
+ * plot2d.py:1008-1011): oa[ir][iz] = mean over the nth[ir] angles
+ * t_i = i*2pi/nth[ir] of the trilinear interpolation (NaN outside) of the
+ * centred array D (p0, p1, p2) with axes X, Y, Z at
+ * (rarr[ir] cos t, rarr[ir] sin t, zar[iz]) * b_inv (b_inv_host: 9 doubles,
+ * row major, host memory).  The host finishes as the reference does (NaN ->
+ * smallest average, division by the mean, mirror to -r).
+ */
+int msf_cyl_average(const double* D, int32_t p0, int32_t p1, int32_t p2, const double* X,
+                    const double* Y, const double* Z, const double* b_inv_host, const double* rarr,
+                    const int32_t* nth, int32_t nr, const double* zar, int32_t nz, double* oa,
+                    msf_stream_t stream);
+
 /* ----------------------------------------------------- direct sum (a13)
  * S_q = |sum_j f_j exp(i q.r_j)|^2 for n_sys systems of n_atoms atoms and
  * n_q vectors each (FP32).  r_f: (n_sys, n_atoms) float4 (x, y, z, f);

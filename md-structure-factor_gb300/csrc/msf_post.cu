@@ -108,9 +108,69 @@ __global__ void k_ewald(const double* __restrict__ D, int p0, int p1, int p2,
   }
 }
 
+// plot2d.py:601-631 (PLOT_RAD_NEW): ring (r, z) of nth angles
+// t_i = i * (2 pi / nth); the point (r cos t, r sin t, z) times b_inv (row
+// vector times matrix), interpolated as RegularGridInterpolator does; the
+// ring average is the mean over its angles (NaN if any sample is outside).
+struct CylArgs {
+  const double* D;
+  int p0, p1, p2;
+  const double* X;
+  const double* Y;
+  const double* Z;
+  double b[9];
+  const double* rarr;
+  const int* nth;
+  int nr;
+  const double* zar;
+  int nz;
+  double* oa;
+};
+
+__global__ void k_cyl(CylArgs a) {
+  const int64_t total = (int64_t)a.nr * a.nz;
+  const double two_pi = 6.283185307179586232;   // the double nearest 2 pi (numpy's np.pi * 2.0)
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int ir = (int)(e / a.nz), iz = (int)(e % a.nz);
+    const double r = __ldg(a.rarr + ir), z = __ldg(a.zar + iz);
+    const int n = __ldg(a.nth + ir);
+    const double step = __ddiv_rn(two_pi, (double)n);
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double t = __dmul_rn((double)i, step);
+      double s, c;
+      sincos(t, &s, &c);
+      const double px = __dmul_rn(r, c), py = __dmul_rn(r, s);
+      const double qx = __dadd_rn(__dadd_rn(__dmul_rn(px, a.b[0]), __dmul_rn(py, a.b[3])), __dmul_rn(z, a.b[6]));
+      const double qy = __dadd_rn(__dadd_rn(__dmul_rn(px, a.b[1]), __dmul_rn(py, a.b[4])), __dmul_rn(z, a.b[7]));
+      const double qz = __dadd_rn(__dadd_rn(__dmul_rn(px, a.b[2]), __dmul_rn(py, a.b[5])), __dmul_rn(z, a.b[8]));
+      sum = __dadd_rn(sum, interp3(a.D, a.p0, a.p1, a.p2, a.X, a.Y, a.Z, qx, qy, qz));
+    }
+    a.oa[e] = __ddiv_rn(sum, (double)n);
+  }
+}
+
 }  // namespace msf
 
 using namespace msf;
+
+extern "C" int msf_cyl_average(const double* D, int32_t p0, int32_t p1, int32_t p2, const double* X,
+                               const double* Y, const double* Z, const double* b_inv_host,
+                               const double* rarr, const int32_t* nth, int32_t nr, const double* zar,
+                               int32_t nz, double* oa, msf_stream_t stream) {
+  if (!D || !X || !Y || !Z || !b_inv_host || !rarr || !nth || !zar || !oa) return MSF_E_INVALID;
+  if (p0 < 2 || p1 < 2 || p2 < 2 || nr < 1 || nz < 1) return MSF_E_INVALID;
+  CylArgs a;
+  a.D = D; a.p0 = p0; a.p1 = p1; a.p2 = p2;
+  a.X = X; a.Y = Y; a.Z = Z;
+  for (int i = 0; i < 9; ++i) a.b[i] = b_inv_host[i];
+  a.rarr = rarr; a.nth = nth; a.nr = nr; a.zar = zar; a.nz = nz; a.oa = oa;
+  const int64_t total = (int64_t)nr * nz;
+  const int blocks = (int)((total + 127) / 128 < 152 * 16 ? (total + 127) / 128 : 152 * 16);
+  k_cyl<<<blocks, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
+  return launch_status();
+}
 
 extern "C" {
 

@@ -74,6 +74,8 @@ SIGNATURES = {
     "msf_gauss_grid_f64": (c_int, [c_p, c_p, c_p, c_i64, c_p, c_int, c_p, c_p, c_p]),
     "msf_sfplt": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p]),
     "msf_ewald": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_d, c_p, c_p, c_p, c_p]),
+    "msf_cyl_average": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_int, c_p, c_int,
+                                c_p, c_p]),
     "msf_direct_fwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p]),
     "msf_direct_bwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p, c_p]),
     "msf_batch_create": (c_int, [C.POINTER(c_p), C.POINTER(BatchSystem), c_int, c_int]),

@@ -252,6 +252,47 @@ def ewald_from_sf(sf, L, wavelength):
     return ewald_slices(D, X, Y, Z, wavelength)
 
 
+def cylindrical_average(D, X, Y, Z, ucell, format=False):
+    """PLOT_RAD_NEW's cylindrical (r, z) average (plot2d.py:578-645) with the
+    ring sums on the GPU.  D: centred S (p0, p1, p2) CUDA float64 (e.g.
+    ``get_dplot(sf)``); X, Y, Z its axes; ucell 3x3.  Returns numpy
+    (final, rfin, zfin, oa) as the reference builds them: 400 radii up to 0.95
+    of half the smaller in-plane q extent, max(int(20*2*pi*r), 1) angles per
+    ring, NaN -> smallest average, division by the mean unless ``format``,
+    mirrored to (-r, r)."""
+    dev = D.device
+    X = np.asarray(X, np.float64)
+    Y = np.asarray(Y, np.float64)
+    Z = np.asarray(Z, np.float64)
+    u = np.asarray(ucell, np.float64)
+    a1, a2, a3 = u[0], u[1], u[2]
+    b1 = (np.cross(a2, a3)) / (np.dot(a1, np.cross(a2, a3)))
+    b2 = (np.cross(a3, a1)) / (np.dot(a2, np.cross(a3, a1)))
+    b3 = (np.cross(a1, a2)) / (np.dot(a3, np.cross(a1, a2)))
+    b_inv = np.ascontiguousarray(np.linalg.inv(np.vstack((b1, b2, b3))))
+    Rmax = min((X[-1] - X[0]) * u[0][0], (Y[-1] - Y[0]) * u[1][1]) / 2.0
+    Rmax *= 0.95
+    rarr = np.linspace(0.0, Rmax, 400)
+    zar = np.linspace(Z[0], Z[-1], Z.shape[0])
+    circ = 2. * np.pi * rarr
+    nth = np.array([max(int(20.0 * c), 1) for c in circ], dtype=np.int32)
+    p0, p1, p2 = D.shape
+    oa = torch.empty((400, Z.shape[0]), dtype=torch.float64, device=dev)
+    Xd, Yd, Zd = (to_device(a, dev) for a in (X, Y, Z))
+    rd, nd, zd = to_device(rarr, dev), to_device(nth, dev), to_device(zar, dev)
+    with torch.cuda.device(dev):
+        call("msf_cyl_average", _ptr(D.contiguous()), p0, p1, p2, _ptr(Xd), _ptr(Yd), _ptr(Zd),
+             c_p(b_inv.ctypes.data), _ptr(rd), _ptr(nd), 400, _ptr(zd), Z.shape[0], _ptr(oa), stream_ptr(dev))
+    o = oa.cpu().numpy()
+    mn = np.nanmin(o)
+    o = np.where(np.isnan(o), mn, o)
+    if not format:
+        o /= np.average(o)
+    final = np.append(o[::-1, :], o[1:], axis=0)
+    rfin = np.append(-rarr[::-1], rarr[1:])
+    return final, rfin, zar, o
+
+
 # ------------------------------------------------------------ direct sum
 def _pack_rf(r, f):
     if f.dim() == r.dim() - 1:

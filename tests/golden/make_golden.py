@@ -186,6 +186,26 @@ def main(ref):
     np.savez_compressed(os.path.join(HERE, "hist_edges.npz"), **hist_edges_case())
     print("hist_edges done")
 
+    # cylindrical (r, z) average of PLOT_RAD_NEW (plot2d.py:559-640), the step
+    # the reference CLI runs after compute_sf (main_gromacs.py:231 ->
+    # plot2d.py:1008-1011); `final` is recorded from its first contourf call.
+    th = 120 * np.pi / 180.0
+    for name, ucell in (("gauss_ortho", np.eye(3)),
+                        ("gauss_tcl", np.array([[1, 0, 0], [np.cos(th), np.sin(th), 0], [0, 0, 1]]))):
+        D = np.load(os.path.join(HERE, name + ".npz"))["out_kgridplt"]
+        del calls[:]
+        with contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
+            plot2d.trange = range
+            try:
+                plot2d.PLOT_RAD_NEW(D, 1.54, ucell, format=False)
+            except Exception:   # plotting tail after the recorded call; not part of the average
+                pass
+        cf = [c for c in calls if c[0] == "contourf"]
+        rfin, zfin0, finalT = cf[0][1][0], cf[0][1][1], cf[0][1][2]
+        np.savez_compressed(os.path.join(HERE, "cyl_" + name.split("_", 1)[1] + ".npz"),
+                            D=D, ucell=ucell, rfin=rfin, zfin=zfin0, final=np.asarray(finalT).T)
+        print("cyl", name, np.asarray(finalT).shape)
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -117,3 +117,13 @@ def test_single_atom_kat():
     pos = np.array([[[0.31, 0.77, 0.12]]], np.float32)
     sf = mdsf.structure_factor(pos, (1.0, 1.0, 1.0), np.array([7], np.int32), (16, 12, 10)).cpu().numpy()
     np.testing.assert_allclose(sf, 49.0, rtol=1e-6)
+
+
+def test_large_grid_512_cubed():
+    """The stress-test grid (512^3, planes larger than shared memory): one frame
+    of a 6 x 6 column system in a 25 nm box against numpy."""
+    pos, box, w = synth.columnar(n_atoms=30_000, box=(25.0, 25.0, 25.0), n_cols=(6, 6), lattice=25.0 / 6,
+                                 frames=1, seed=4)
+    ref = ohist.hist_sf(pos, box, w, (512, 512, 512))
+    got = mdsf.structure_factor(pos, box, w, (512, 512, 512), tuning=dict(batch=1)).cpu().numpy()
+    assert rel_err(got, ref) < TOL

@@ -56,3 +56,15 @@ def test_ewald_from_sf_chain():
     xy, xz, yz = mdsf.ewald_from_sf(torch.from_numpy(z["out_sf"]).cuda(), z["out_L"], 1.54)
     np.testing.assert_allclose(xy.cpu().numpy(), e["xy"], rtol=1e-12)
     np.testing.assert_allclose(yz.cpu().numpy(), e["yz"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["ortho", "tcl"])
+def test_cylindrical_average_vs_reference(name):
+    """PLOT_RAD_NEW's (r, z) ring average on the GPU against the reference's own output."""
+    z = np.load(os.path.join(GOLDEN, "cyl_" + name + ".npz"))
+    D = z["D"]
+    final, rfin, zfin, oa = mdsf.cylindrical_average(torch.from_numpy(np.ascontiguousarray(D[..., 3])).cuda(),
+                                                     D[:, 0, 0, 0], D[0, :, 0, 1], D[0, 0, :, 2], z["ucell"])
+    np.testing.assert_array_equal(rfin, z["rfin"])
+    np.testing.assert_array_equal(zfin, z["zfin"])
+    np.testing.assert_allclose(final, z["final"], rtol=1e-11, atol=0)

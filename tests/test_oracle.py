@@ -122,3 +122,13 @@ def test_hist_two_atoms_kat():
     k = np.arange(n[0])
     expect = 9 + 25 + 30 * np.cos(2 * np.pi * k / n[0])
     np.testing.assert_allclose(sf[:, 0, 0], expect, rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["ortho", "tcl"])
+def test_cylindrical_average_restatement_matches_reference(name):
+    from oracle import cyl as ocyl
+    z = load("cyl_" + name)
+    final, rfin, zfin, _ = ocyl.cylindrical_average(z["D"], z["ucell"])
+    np.testing.assert_array_equal(rfin, z["rfin"])
+    np.testing.assert_array_equal(zfin, z["zfin"])
+    np.testing.assert_allclose(final, z["final"], rtol=1e-12, atol=0)
