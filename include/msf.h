@@ -177,7 +177,11 @@ int msf_hist_sf_f64(msf_plan* plan, const double* pos, const int32_t* weights, i
  *   type_tab:   (n_types, 5) doubles: c1 = Nel/sigma^3, c2 = 2*sigma^2,
  *               Ax, Ay, Az (the int() of the get_borders widths,
  *               dens.py:38-43, 287; c1, c2 as dens.py:308 computes them).
- *   geom:       16 doubles: dr[3], ucell[9] (row major), nborder, 0, 0, 0.
+ *   geom:       16 doubles (host): dr[3], ucell[9] (row major), nborder,
+ *               the largest footprint 2*max(A) over the types (0 = unknown:
+ *               use the direct per-voxel exp), 0, 0.  With a footprint of at
+ *               most 64 the density is evaluated in separable form (1-D and
+ *               cross-term 2-D factor tables per atom; equal up to rounding).
  */
 int msf_gauss_grid_f64(const msf_plan* plan, const double* pos, const int32_t* type_index,
                        int64_t n_atoms, const double* type_tab, int32_t n_types,

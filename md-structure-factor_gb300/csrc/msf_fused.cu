@@ -232,8 +232,13 @@ __global__ void __maxnreg__((PlaneShape<N1, N2>::NT >= 512 ? 80 : 128)) k_plane_
   r2::fft2_lines<N2, P, SP, 1, NT>(buf, twz);    // z: lines = pairs p, samples stride SP
   r2::fft2_lines<P, N2, 1, SP, NT>(buf, twp);    // half y: lines = kz, samples stride 1
   float2* out = a.C + frame * a.Vh + (int64_t)x * N1 * NH;
-  for (int e = threadIdx.x; e < P * NH; e += NT) {
-    const int q = e / NH, k = e % NH;
+  // 2-D real split.  Columns k < N2/2: thread (k = tid % KC, g = tid / KC)
+  // takes rows q = g, g + QS, ... so addresses advance by constants; a warp
+  // covers consecutive k (coalesced stores, stride-SP shared loads).  The
+  // Nyquist column k = N2/2 follows.
+  constexpr int KC = N2 / 2 < NT ? N2 / 2 : NT;   // columns per sweep
+  constexpr int QS = NT / KC;                     // rows advanced per step
+  auto split = [&](int q, int k) {
     const int kn = (N2 - k) & (N2 - 1);
     const int qn = (P - q) & (P - 1);
     const float2 w = buf[k * SP + q];
@@ -243,7 +248,12 @@ __global__ void __maxnreg__((PlaneShape<N1, N2>::NT >= 512 ? 80 : 128)) k_plane_
     const float2 t = cmul(twy[q], O);
     out[q * NH + k] = cadd(E, t);
     out[(q + P) * NH + k] = csub(E, t);
+  };
+  for (int k = threadIdx.x % KC; k < N2 / 2; k += KC) {
+#pragma unroll 4
+    for (int q = threadIdx.x / KC; q < P; q += QS) split(q, k);
   }
+  for (int q = threadIdx.x; q < P; q += NT) split(q, N2 / 2);
 }
 
 // ------------------------------------------------- x pass + |F|^2 + sum

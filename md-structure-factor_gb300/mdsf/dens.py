@@ -178,6 +178,7 @@ def compute_sf_arrays(r, L, typ, rad, ucell, Sres, mode="gauss", device=None):
             geom[0:3] = dr
             geom[3:12] = np.asarray(ucell, np.float64).reshape(9)
             geom[12] = nborder
+            geom[13] = 2 * int(tab[:, 2:5].max())   # largest footprint: separable evaluation when <= 64
             geom_c = _ptr_np(geom)
             td = to_device(tidx, device)
             tabd = to_device(tab, device)

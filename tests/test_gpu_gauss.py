@@ -44,9 +44,11 @@ def test_compute_sf_gauss_matches_reference(name, tmp_path):
     np.testing.assert_array_equal(got["kgridplt"][..., :3], z["out_kgridplt"][..., :3])
 
 
+@pytest.mark.parametrize("separable", [False, True])
 @pytest.mark.parametrize("name", NAMES)
-def test_gauss_density_fp64(name):
-    """The folded FP64 density of frame 0 against the oracle at 1e-12."""
+def test_gauss_density_fp64(name, separable):
+    """The folded FP64 density of frame 0 against the oracle at 1e-12, by the
+    direct per-voxel exp and by the separable factor tables."""
     z, rad = case(name)
     r = z["r"].copy()
     r, Lm = odens.rescale(r, z["L_in"].copy())
@@ -64,6 +66,7 @@ def test_gauss_density_fp64(name):
     geom[0:3] = dr
     geom[3:12] = z["ucell"].reshape(9)
     geom[12] = nb
+    geom[13] = 2 * int(tab[:, 2:5].max()) if separable else 0
     grid = torch.empty(dims, dtype=torch.float64, device="cuda")
     rd = torch.from_numpy(np.ascontiguousarray(r[0])).cuda()
     td = torch.from_numpy(tidx).cuda()
