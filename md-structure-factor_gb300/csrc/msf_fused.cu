@@ -20,6 +20,11 @@
 //                    columns for every frame of the batch, |F|^2 summed over
 //                    the batch in FP32, one FP64 RMW of sf.
 // All FFT lengths are template constants (msf_r2.cuh, msf_ct.cuh).
+#include <math.h>
+
+#include <atomic>
+#include <vector>
+
 #include "msf_bins.cuh"
 #include "msf_ct.cuh"
 #include "msf_r2.cuh"
@@ -130,53 +135,203 @@ struct PlaneCtArgs {
   const float2* twy;
 };
 
+// Twiddles w_N^k (k < N) of the plane kernel for N = 16, 32, ..., 512, at
+// offset N - 16, in constant memory: every index the plane kernel uses is
+// uniform across a warp, so the table costs no shared-memory bandwidth (the
+// plane FFT is bound by shared-memory wavefronts).  Filled once per device
+// by plane_twiddles_init (msf_plan_bind).
+constexpr int kConstTw = 1024 - 16;
+__constant__ float2 c_tw[kConstTw];
+
+template <int N>
+struct CTw {
+  static_assert(N >= 16 && N <= 512 && (N & (N - 1)) == 0, "constant twiddles: N = 16..512");
+  __device__ __forceinline__ float2 operator()(int k) const { return c_tw[N - 16 + k]; }
+};
+
 template <int N1, int N2>
 struct PlaneShape {
   static constexpr int P = N1 / 2;
   static constexpr int SP = P + 1;      // odd line stride: conflict-free columns
   static constexpr int NH = N2 / 2 + 1;
   static constexpr int NT = (N2 * P >= 4096) ? 512 : 256;
-  // plane, twiddles, then the segment tables of the bucket gather
-  static constexpr size_t SMEM = (size_t)N2 * SP * sizeof(float2) + (size_t)(N2 + 2 * P) * sizeof(float2) +
-                                 (size_t)(2 * NT + 1 + NT / 32) * sizeof(int);
+  // plane, then the segment tables of the bucket gather
+  static constexpr size_t SMEM = (size_t)N2 * SP * sizeof(float2) + (size_t)(2 * NT + 1 + NT / 32) * sizeof(int);
 };
 
-// SRC 0: atoms from the plane's bucket; SRC 1: a dense grid (int32/float32/float64)
-// Registers capped so that one x-pass CTA fits on the SM beside a plane CTA
-// (the two kernels overlap on different streams).
-template <int N1, int N2, int SRC>
-__global__ void __maxnreg__((PlaneShape<N1, N2>::NT >= 512 ? 80 : 128)) k_plane_ct(PlaneCtArgs a) {
+// Last pass of the half-length y FFT fused with the 2-D real split.  After
+// r2::pass1_fn, DFT_A over the slots A*k1 + n1 of kz line l gives
+// W[q = k1 + B*k2][l] (k2 < A).  The split pairs W[q][k] with W[-q][-k]:
+// for k1 != 0 that is k2' = A-1-k2 of item (B-k1, -l), for k1 == 0 it is
+// k2' = (A-k2) mod A of item (0, -l).  A unit is two items transformed in
+// registers and written straight to the half plane:
+//   interior line l (0 < l < n2/2): item (k1, l) and its partner on line -l
+//     (only the first is an output);
+//   edge line l = 0 or n2/2, 0 < k1 < B/2: items (k1, l) and (B-k1, l), each
+//     the other's partner, both outputs;
+//   edge line, k1 = 0 and B/2: two self-paired items in one unit.
+// That is B*n2/2 units of equal transform work: exactly two per thread at
+// the headline size, with no tail.  Edge units come first.
+template <int N1, int N2, int SP, int NT>
+__device__ __forceinline__ void ypass2_split(const float2* buf, float2* out) {
+  constexpr int P = N1 / 2, NH = N2 / 2 + 1;
+  constexpr int A = r2::Split2<P>::A, B = r2::Split2<P>::B;
+  constexpr int KM = N2 / 2 - 1;          // interior output lines 1 .. n2/2 - 1
+  constexpr int U = B * (N2 / 2);         // B edge units + B*KM interior units
+  const CTw<N1> wq;
+  auto emit = [&](int q, int k, float2 w, float2 wm_raw) {
+    const float2 wm = cconj(wm_raw);
+    const float2 E = cscale(cadd(w, wm), 0.5f);
+    const float2 O = cscale(cmi(csub(w, wm)), 0.5f);
+    const float2 t = cmul(wq(q), O);
+    __stcs(out + q * NH + k, cadd(E, t));   // evict-first: keep L2 for the bucket entries
+    __stcs(out + (q + P) * NH + k, csub(E, t));
+  };
+  for (int u = threadIdx.x; u < U; u += NT) {
+    int l, lp, k1, k1p;
+    if (u < B) {                     // edge line: j = 0 pairs the two self-paired items
+      l = lp = u < B / 2 ? 0 : N2 / 2;
+      k1 = u % (B / 2);
+      k1p = k1 ? B - k1 : B / 2;
+    } else {
+      k1 = (u - B) / KM;
+      l = 1 + (u - B) % KM;
+      lp = N2 - l;
+      k1p = (B - k1) & (B - 1);
+    }
+    const float2* pa = buf + l * SP + A * k1;
+    const float2* pb = buf + lp * SP + A * k1p;
+    float2 a[A], b[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) { a[n1] = pa[n1]; b[n1] = pb[n1]; }
+    reg::reg_dft<A>(a);
+    reg::reg_dft<A>(b);
+    if (u < B && k1 == 0) {
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) emit(B * k2, l, a[k2], a[(A - k2) & (A - 1)]);
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) emit(B / 2 + B * k2, l, b[k2], b[A - 1 - k2]);
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) emit(k1 + B * k2, l, a[k2], b[k1 ? A - 1 - k2 : (A - k2) & (A - 1)]);
+      if (u < B) {
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) emit(k1p + B * k2, l, b[k2], a[A - 1 - k2]);
+      }
+    }
+  }
+}
+
+// z FFT of the row pairs, then the half-length y FFT with the real split:
+// the deposited plane in buf becomes the half plane at out.
+template <int N1, int N2>
+__device__ __forceinline__ void plane_transform(float2* buf, float2* out) {
   using S = PlaneShape<N1, N2>;
-  constexpr int P = S::P, SP = S::SP, NH = S::NH, NT = S::NT;
+  // z: lines = pairs p, samples stride SP; then pass 1 of the half y FFT
+  // (lines = kz, samples stride 1), and its pass 2 fused with the real split
+  r2::fft2_lines_fn<N2, S::P, S::SP, 1, S::NT>(buf, CTw<N2>());
+  r2::pass1_fn<S::P, N2, 1, S::SP, S::NT>(buf, CTw<S::P>());
+  __syncthreads();
+  ypass2_split<N1, N2, S::SP, S::NT>(buf, out);
+}
+
+// float offset of voxel y*n2 + z in the row-pair layout buf[z][p].(y & 1)
+template <int N2, int SP>
+__device__ __forceinline__ int pair_offset(int vx) {
+  const int y = vx / N2, z = vx % N2;
+  return 2 * (z * SP + (y >> 1)) + (y & 1);
+}
+
+// Registers capped so that one x-pass CTA (256 threads x 80) fits on the SM
+// beside a 512-thread plane CTA (the two kernels overlap on different
+// streams): 80 for the grid-source kernel, 88 for the bucket kernel, which
+// also carries the next plane's entries (512 x 88 + 256 x 80 = 65536).  Not
+// where the fused y pass holds two 16-point transforms (n1 = 512).
+#define MSF_PLANE_MAXNREG(N1, N2, CAP) (PlaneShape<N1, N2>::NT >= 512 && r2::Split2<N1 / 2>::A < 16 ? CAP : 128)
+
+// Dense-grid source (int32 / float32 / float64 grids of a batch): one CTA
+// per (x, frame).
+template <int N1, int N2>
+__global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneCtArgs a) {
+  using S = PlaneShape<N1, N2>;
+  constexpr int SP = S::SP, NT = S::NT;
   extern __shared__ float2 smem[];
   float2* buf = smem;                 // [N2][SP], z major
-  float2* twz = buf + N2 * SP;        // N2
-  float2* twp = twz + N2;             // P
-  float2* twy = twp + P;              // P (w^q, q < P)
-  int* bufi = reinterpret_cast<int*>(buf);
   float* buff = reinterpret_cast<float*>(buf);
   const int x = blockIdx.x;
   const int frame = blockIdx.y;
-  for (int i = threadIdx.x; i < N2; i += NT) twz[i] = a.twz[i];
-  for (int i = threadIdx.x; i < P; i += NT) { twp[i] = a.twp[i]; twy[i] = a.twy[i]; }
-  if (SRC == 0) {
-    // The plane's atoms sit in one segment per bucketing block.  Thread t
-    // loads segment t's bounds first (the loads overlap the zeroing below);
-    // a block scan of the segment lengths then lets every thread fetch one
-    // entry of the concatenated segments in a single round of loads.
-    int* seg_start = reinterpret_cast<int*>(twy + P);   // NT + 1 ints
-    int* seg_lo = seg_start + NT + 1;                   // NT ints
-    int* warp_sum = seg_lo + NT;                        // NT / 32 ints
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool flat = a.nblk <= NT;
-    int lo = 0, cnt = 0;
-    if (flat && tid < a.nblk) {
-      const int* bo = a.boff + ((int64_t)frame * a.nblk + tid) * (a.n0 + 1);
-      lo = bo[x];
-      cnt = bo[x + 1] - lo;
-    }
-    int4* z4 = reinterpret_cast<int4*>(buf);
-    for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
+  const int64_t g0 = frame * a.V + (int64_t)x * N1 * N2;
+  for (int e = threadIdx.x; e < N1 * N2; e += NT) {
+    float v;
+    if (a.grid_kind == kGridI32) v = (float)__ldg(static_cast<const int32_t*>(a.grids) + g0 + e);
+    else if (a.grid_kind == kGridF32) v = __ldg(static_cast<const float*>(a.grids) + g0 + e);
+    else v = (float)__ldg(static_cast<const double*>(a.grids) + g0 + e);
+    buff[pair_offset<N2, SP>(e)] = v;
+  }
+  __syncthreads();
+  plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
+}
+
+// Bucket source, persistent: CTA b transforms planes (frame, x) = item b,
+// b + gridDim.x, ... of the batch.  Plane x's atoms sit in one segment per
+// bucketing block; a block scan of the segment lengths (thread t owns
+// segment t) gives the segment tables, and thread t then deposits entries
+// t, t + NT, ... of the concatenated segments.  Before the FFT of plane i,
+// every thread cp.async-copies its own segment of plane i + G to its place in
+// the concatenation (up to kPlanePrefetch*NT entries are staged; the rest are
+// read at deposit time through the tables), and the raw bounds of its
+// segment of plane i + 2G (G = gridDim.x), so their global-memory latency is
+// spent under the FFT instead of between planes.
+constexpr int kPlanePrefetch = 2;
+
+template <int N1, int N2>
+struct BucketPlaneShape {
+  using S = PlaneShape<N1, N2>;
+  static constexpr int NT = S::NT, R = kPlanePrefetch;
+  // plane, segment tables (2 NT + 1 + NT/32 ints, padded to 8 bytes), raw
+  // bounds (NT int2), staged entries (R NT int2)
+  static constexpr size_t TAB_INTS = (2 * NT + 1 + NT / 32 + 1) & ~(size_t)1;
+  static constexpr size_t SMEM = (size_t)N2 * S::SP * sizeof(float2) + TAB_INTS * sizeof(int) +
+                                 (size_t)(NT + R * NT) * sizeof(int2);
+};
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N1, int N2>
+__global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtArgs a, int items) {
+  using S = PlaneShape<N1, N2>;
+  using BS = BucketPlaneShape<N1, N2>;
+  constexpr int SP = S::SP, NT = S::NT, R = kPlanePrefetch;
+  extern __shared__ float2 smem[];
+  float2* buf = smem;                                       // [N2][SP], z major
+  float* buff = reinterpret_cast<float*>(buf);
+  int* seg_start = reinterpret_cast<int*>(buf + N2 * SP);   // NT + 1 ints
+  int* seg_lo = seg_start + NT + 1;                         // NT ints
+  int* warp_sum = seg_lo + NT;                              // NT / 32 ints
+  int2* sbounds = reinterpret_cast<int2*>(seg_start + BS::TAB_INTS);   // NT: (bo[x], bo[x + 1])
+  int2* staged = sbounds + NT;                              // R * NT entries
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool flat = a.nblk <= NT;
+  const int G = gridDim.x;
+  auto has_segment = [&](int item) { return flat && item < items && tid < a.nblk; };
+  auto bounds_ptr = [&](int item) {
+    const int frame = item / a.n0, x = item - frame * a.n0;
+    return a.boff + ((int64_t)frame * a.nblk + tid) * (a.n0 + 1) + x;
+  };
+  // block scan of the segment lengths into the tables (two barriers);
+  // returns the entry count, `start` gets this thread's segment start
+  auto tables = [&](int lo, int cnt, int& start) {
     int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -185,75 +340,101 @@ __global__ void __maxnreg__((PlaneShape<N1, N2>::NT >= 512 ? 80 : 128)) k_plane_
     }
     if (lane == 31) warp_sum[warp] = incl;
     __syncthreads();
-    int before = 0;
-    for (int w = 0; w < warp; ++w) before += warp_sum[w];
-    seg_start[tid] = before + incl - cnt;
+    int ws = lane < NT / 32 ? warp_sum[lane] : 0;   // exclusive scan of the warp sums
+#pragma unroll
+    for (int o = 1; o < NT / 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    const int before = warp ? __shfl_sync(0xffffffffu, ws, warp - 1) : 0;
+    start = before + incl - cnt;
+    seg_start[tid] = start;
     seg_lo[tid] = lo;
     if (tid == NT - 1) seg_start[NT] = before + incl;
+    __syncthreads();
+    return seg_start[NT];
+  };
+  auto entry_ptr = [&](int item, int e) {   // needs the tables of `item`
+    int s0 = 0, s1 = a.nblk - 1;            // last segment with seg_start <= e
+    while (s0 < s1) {
+      const int m = (s0 + s1 + 1) >> 1;
+      if (seg_start[m] <= e) s0 = m; else s1 = m - 1;
+    }
+    const int frame = item / a.n0;
+    return a.bucket + ((int64_t)frame * a.nblk + s0) * kBucketAtoms + seg_lo[s0] + (e - seg_start[s0]);
+  };
+  // async copies: thread t copies its own segment of `item` (bounds lo, cnt,
+  // concatenated position start) into the staging area, up to its capacity,
+  // and the raw bounds of its segment of `later`
+  auto stage = [&](int item, int lo, int cnt, int start, int later) {
+    if (cnt > 0) {
+      const int frame = item / a.n0;
+      const int2* src = a.bucket + ((int64_t)frame * a.nblk + tid) * kBucketAtoms + lo;
+      const int n = min(cnt, R * NT - start);
+      for (int j = 0; j < n; ++j) cp_async8(staged + start + j, src + j);
+    }
+    if (has_segment(later)) {
+      const int* bo = bounds_ptr(later);
+      cp_async4(&sbounds[tid].x, bo);
+      cp_async4(&sbounds[tid].y, bo + 1);
+    }
+    cp_async_commit();
+  };
+
+  int item = blockIdx.x;
+  int total;
+  {
+    int lo = 0, cnt = 0, start;
+    if (has_segment(item)) {
+      const int* bo = bounds_ptr(item);
+      lo = bo[0];
+      cnt = bo[1] - lo;
+    }
+    total = tables(lo, cnt, start);
+    stage(item, lo, cnt, start, item + G);
+  }
+
+  for (; item < items; item += G) {
+    const int frame = item / a.n0, x = item - frame * a.n0;
+    int4* z4 = reinterpret_cast<int4*>(buf);
+    for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
+    cp_async_commit_wait_all();
     __syncthreads();
     // integer weights summed in FP32: exact (and order-independent) while a
     // voxel's total stays below 2^24 electrons
     if (flat) {
-      const int total = seg_start[NT];
       for (int e = tid; e < total; e += NT) {
-        int s0 = 0, s1 = a.nblk - 1;     // last segment with seg_start <= e
-        while (s0 < s1) {
-          const int m = (s0 + s1 + 1) >> 1;
-          if (seg_start[m] <= e) s0 = m; else s1 = m - 1;
-        }
-        const int2 v = a.bucket[((int64_t)frame * a.nblk + s0) * kBucketAtoms + seg_lo[s0] + (e - seg_start[s0])];
-        const int y = v.x / N2, z = v.x % N2;
-        atomicAdd(buff + 2 * (z * SP + (y >> 1)) + (y & 1), (float)v.y);
+        const int2 v = e < R * NT ? staged[e] : *entry_ptr(item, e);
+        atomicAdd(buff + pair_offset<N2, SP>(v.x), (float)v.y);
       }
     } else {
+      // more bucketing blocks than threads: a warp per block, no staging
       for (int blk = warp; blk < a.nblk; blk += NT / 32) {
         const int* bo = a.boff + ((int64_t)frame * a.nblk + blk) * (a.n0 + 1);
         const int e0 = bo[x], e1 = bo[x + 1];
         const int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
         for (int e = e0 + lane; e < e1; e += 32) {
           const int2 v = bk[e];
-          const int y = v.x / N2, z = v.x % N2;
-          atomicAdd(buff + 2 * (z * SP + (y >> 1)) + (y & 1), (float)v.y);
+          atomicAdd(buff + pair_offset<N2, SP>(v.x), (float)v.y);
         }
       }
     }
-  } else {
-    const int64_t g0 = frame * a.V + (int64_t)x * N1 * N2;
-    for (int e = threadIdx.x; e < N1 * N2; e += NT) {
-      const int y = e / N2, z = e % N2;
-      float v;
-      if (a.grid_kind == kGridI32) v = (float)__ldg(static_cast<const int32_t*>(a.grids) + g0 + e);
-      else if (a.grid_kind == kGridF32) v = __ldg(static_cast<const float*>(a.grids) + g0 + e);
-      else v = (float)__ldg(static_cast<const double*>(a.grids) + g0 + e);
-      buff[2 * (z * SP + (y >> 1)) + (y & 1)] = v;
+    __syncthreads();
+    // next plane: tables from the staged bounds, then its entries and the
+    // bounds of the plane after it are copied while this plane transforms
+    const int next = item + G;
+    int lo = 0, cnt = 0, start;
+    if (has_segment(next)) {
+      const int2 b = sbounds[tid];
+      lo = b.x;
+      cnt = b.y - b.x;
     }
+    total = tables(lo, cnt, start);
+    stage(next, lo, cnt, start, next + G);
+    plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
+    __syncthreads();   // the split has read buf before it is zeroed again
   }
-  __syncthreads();
-  r2::fft2_lines<N2, P, SP, 1, NT>(buf, twz);    // z: lines = pairs p, samples stride SP
-  r2::fft2_lines<P, N2, 1, SP, NT>(buf, twp);    // half y: lines = kz, samples stride 1
-  float2* out = a.C + frame * a.Vh + (int64_t)x * N1 * NH;
-  // 2-D real split.  Columns k < N2/2: thread (k = tid % KC, g = tid / KC)
-  // takes rows q = g, g + QS, ... so addresses advance by constants; a warp
-  // covers consecutive k (coalesced stores, stride-SP shared loads).  The
-  // Nyquist column k = N2/2 follows.
-  constexpr int KC = N2 / 2 < NT ? N2 / 2 : NT;   // columns per sweep
-  constexpr int QS = NT / KC;                     // rows advanced per step
-  auto split = [&](int q, int k) {
-    const int kn = (N2 - k) & (N2 - 1);
-    const int qn = (P - q) & (P - 1);
-    const float2 w = buf[k * SP + q];
-    const float2 wm = cconj(buf[kn * SP + qn]);
-    const float2 E = cscale(cadd(w, wm), 0.5f);
-    const float2 O = cscale(cmi(csub(w, wm)), 0.5f);
-    const float2 t = cmul(twy[q], O);
-    out[q * NH + k] = cadd(E, t);
-    out[(q + P) * NH + k] = csub(E, t);
-  };
-  for (int k = threadIdx.x % KC; k < N2 / 2; k += KC) {
-#pragma unroll 4
-    for (int q = threadIdx.x / KC; q < P; q += QS) split(q, k);
-  }
-  for (int q = threadIdx.x; q < P; q += NT) split(q, N2 / 2);
+  cp_async_commit_wait_all();   // no copy left in flight into shared memory at exit
 }
 
 // ------------------------------------------------- x pass + |F|^2 + sum
@@ -319,6 +500,9 @@ template <typename K>
 static void allow_smem_once(K kernel, bool& once) {
   if (!once) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    // the whole unified L1/shared array as shared memory, so an x-pass CTA
+    // finds room beside a plane CTA
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     once = true;
   }
 }
@@ -327,13 +511,20 @@ template <int N1, int N2>
 static int launch_plane_ct(const PlaneCtArgs& a, int src, int n0, int nframes, cudaStream_t st) {
   using S = PlaneShape<N1, N2>;
   static bool once0 = false, once1 = false;
-  dim3 grid(n0, nframes);
+  static int sms = 0;
   if (src == 0) {
-    allow_smem_once(k_plane_ct<N1, N2, 0>, once0);
-    k_plane_ct<N1, N2, 0><<<grid, S::NT, S::SMEM, st>>>(a);
+    allow_smem_once(k_plane_ct<N1, N2>, once0);
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (sms <= 0) sms = 152;
+    }
+    const int items = n0 * nframes;
+    k_plane_ct<N1, N2><<<items < sms ? items : sms, S::NT, BucketPlaneShape<N1, N2>::SMEM, st>>>(a, items);
   } else {
-    allow_smem_once(k_plane_ct<N1, N2, 1>, once1);
-    k_plane_ct<N1, N2, 1><<<grid, S::NT, S::SMEM, st>>>(a);
+    allow_smem_once(k_plane_grid<N1, N2>, once1);
+    k_plane_grid<N1, N2><<<dim3(n0, nframes), S::NT, S::SMEM, st>>>(a);
   }
   return launch_status();
 }
@@ -384,6 +575,40 @@ int ct_x_width(int n0, int requested) {
   MSF_X_CASES(X)
 #undef X
   return best;
+}
+
+// w_N^k = exp(-2 pi i k/N) rounded to float: cos/sin in double of the angle
+// reduced to the first quadrant (so 0 and +-1 come out exact), then rotated.
+static std::vector<float2> plane_twiddle_table() {
+  std::vector<float2> t(kConstTw);
+  for (int n = 16; n <= 512; n *= 2) {
+    const int q4 = n / 4;
+    for (int k = 0; k < n; ++k) {
+      const int j = k % q4, quad = k / q4;
+      const double ang = 2.0 * M_PI * (double)j / (double)n;
+      const double c0 = j ? cos(ang) : 1.0, s0 = j ? sin(ang) : 0.0;
+      double c, s;
+      switch (quad) {
+        case 0: c = c0; s = s0; break;
+        case 1: c = -s0; s = c0; break;
+        case 2: c = -c0; s = -s0; break;
+        default: c = s0; s = -c0; break;
+      }
+      t[n - 16 + k] = make_float2((float)c, (float)(-s));
+    }
+  }
+  return t;
+}
+
+int plane_twiddles_init() {
+  static const std::vector<float2> table = plane_twiddle_table();
+  static std::atomic<bool> ready[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return MSF_E_CUDA;
+  if (dev >= 0 && dev < 64 && ready[dev].load(std::memory_order_acquire)) return MSF_OK;
+  if (cudaMemcpyToSymbol(c_tw, table.data(), kConstTw * sizeof(float2)) != cudaSuccess) return MSF_E_CUDA;
+  if (dev >= 0 && dev < 64) ready[dev].store(true, std::memory_order_release);
+  return MSF_OK;
 }
 
 size_t ct_plane_smem(int n1, int n2) {

@@ -283,6 +283,7 @@ int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, i
 // destroys the streams/events a bind created (idempotent)
 void plan_release(msf_plan* p);
 // x pass with TMA tile loads (msf_xtma.cu); prepared at bind time
+int plane_twiddles_init();               // constant-memory twiddles of the plane kernel, once per device
 bool xtma_ok(int n0, int w);
 int xtma_prepare(msf_plan* p);
 int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf);

@@ -272,6 +272,10 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
       if (cudaEventCreateWithFlags(&p->ev_x[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
     }
   }
+  if (p->variant == 3) {
+    s = plane_twiddles_init();
+    if (s) return s;
+  }
   s = xtma_prepare(p);
   if (s) return s;
   p->bound = 1;

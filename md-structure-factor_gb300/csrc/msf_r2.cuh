@@ -26,12 +26,14 @@ template <> struct Split2<128> { static constexpr int B = 16, A = 8; };
 template <> struct Split2<256> { static constexpr int B = 16, A = 16; };
 template <> struct Split2<512> { static constexpr int B = 32, A = 16; };
 
-// Pass 1 over every (n1, l) item.  tw: w_N^k, k < N, in shared memory.
-template <int N, int NL, int SM, int SL, int NT>
-__device__ __forceinline__ void pass1(float2* s, const float2* tw) {
+// Pass 1 over every (n1, l) item.  tw(k) = w_N^k, k < N.  With NL >= 32 the
+// lanes of a warp share n1, so the twiddle index is warp-uniform (a constant
+// memory table then costs no shared-memory bandwidth).
+template <int N, int NL, int SM, int SL, int NT, typename TW>
+__device__ __forceinline__ void pass1_fn(float2* s, TW tw) {
   constexpr int A = Split2<N>::A, B = Split2<N>::B;
   constexpr int ITEMS = A * NL;
-#pragma unroll
+#pragma unroll 1
   for (int base_it = 0; base_it < ITEMS; base_it += NT) {
     const int it = base_it + threadIdx.x;
     if (ITEMS % NT == 0 || it < ITEMS) {
@@ -42,18 +44,24 @@ __device__ __forceinline__ void pass1(float2* s, const float2* tw) {
       for (int n2 = 0; n2 < B; ++n2) v[n2] = p[n2 * A * SM];
       reg::reg_dft<B>(v);
 #pragma unroll
-      for (int k1 = 1; k1 < B; ++k1) v[k1] = cmul(v[k1], tw[n1 * k1]);
+      for (int k1 = 1; k1 < B; ++k1) v[k1] = cmul(v[k1], tw(n1 * k1));
 #pragma unroll
       for (int k1 = 0; k1 < B; ++k1) p[k1 * A * SM] = v[k1];
     }
   }
 }
 
-// Full transform, natural order in and out; ends with a barrier.
+// tw: w_N^k, k < N, in shared memory.
 template <int N, int NL, int SM, int SL, int NT>
-__device__ __forceinline__ void fft2_lines(float2* s, const float2* tw) {
+__device__ __forceinline__ void pass1(float2* s, const float2* tw) {
+  pass1_fn<N, NL, SM, SL, NT>(s, [tw](int k) { return tw[k]; });
+}
+
+// Full transform, natural order in and out; ends with a barrier.
+template <int N, int NL, int SM, int SL, int NT, typename TW>
+__device__ __forceinline__ void fft2_lines_fn(float2* s, TW tw) {
   constexpr int A = Split2<N>::A, B = Split2<N>::B;
-  pass1<N, NL, SM, SL, NT>(s, tw);
+  pass1_fn<N, NL, SM, SL, NT>(s, tw);
   __syncthreads();
   constexpr int ITEMS = B * NL;
   constexpr int PER = (ITEMS + NT - 1) / NT;
@@ -80,6 +88,11 @@ __device__ __forceinline__ void fft2_lines(float2* s, const float2* tw) {
     }
   }
   __syncthreads();
+}
+
+template <int N, int NL, int SM, int SL, int NT>
+__device__ __forceinline__ void fft2_lines(float2* s, const float2* tw) {
+  fft2_lines_fn<N, NL, SM, SL, NT>(s, [tw](int k) { return tw[k]; });
 }
 
 }  // namespace r2

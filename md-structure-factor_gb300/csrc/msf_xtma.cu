@@ -180,6 +180,8 @@ static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs
   static int grid = 0, sms = 0;
   if (!grid) {
     cudaFuncSetAttribute(k_xpower_tma<N0, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    cudaFuncSetAttribute(k_xpower_tma<N0, W>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
     int dev = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -109,3 +109,17 @@ def test_too_many_atoms_for_the_plan():
 def test_headline_plan_uses_tma_x_pass():
     plan = mdsf.get_plan((256, 256, 128), (16.0, 13.856, 8.0), max_atoms=1000, variant=3, batch=4)
     assert plan.tma and plan.tile_w == 16
+
+
+@pytest.mark.parametrize("dims", [(64, 64, 64), (128, 64, 32), (256, 32, 64)])
+@pytest.mark.parametrize("options", [0, 1])
+def test_tma_x_pass_many_frames_per_launch(dims, options):
+    """12 frames per launch through the TMA x pass; options=1 (no overlap)
+    launches more x-pass CTAs per SM."""
+    box = np.array([2.0, 2.2, 1.9])
+    pos, _, w = synth.uniform_system(3_000, box, frames=12, seed=7 + options)
+    ref = ohist.hist_sf(pos, box, w, dims)
+    tuning = dict(batch=12, variant=3, options=options)
+    assert mdsf.get_plan(dims, box, max_atoms=3_000, **tuning).tma
+    got = mdsf.structure_factor(pos, box, w, dims, tuning=tuning).cpu().numpy()
+    assert np.abs(got - ref).max() / ref.max() < TOL
