@@ -243,7 +243,7 @@ def main():
              _ptr(ew[0]), _ptr(ew[1]), _ptr(ew[2]), sp)
 
     batches = (FRAMES + plan.batch - 1) // plan.batch
-    launches_per_step = batches * {1: 3, 2: 4, 3: 3}[plan.variant] + 2
+    launches_per_step = batches * {1: 3, 2: 4, 3: 5}[plan.variant] + 2
 
     # warm-up (also primes one-time kernel attributes before graph capture)
     for _ in range(2):
@@ -329,11 +329,13 @@ def main():
     # compulsory bytes of each stage for one launch of `B` frames
     if plan.variant == 3:
         stage_bytes = {
-            1: lambda k: 16 * N_ATOMS * k + 8 * N_ATOMS * k,       # positions read, bucket entries written
+            # positions read, bucket entries written, then read and written once more compacted
+            1: lambda k: 16 * N_ATOMS * k + 8 * N_ATOMS * k + 16 * N_ATOMS * k,
             2: lambda k: 8 * N_ATOMS * k + 8 * Vh * k,              # bucket read, spectrum written
             4: lambda k: 8 * Vh * k + 16 * Vh,                      # spectrum read, sf read + written
         }
-        stage_names = {1: "k_bucket_sort", 2: "k_plane_ct", 4: "k_xpower_tma" if plan.tma else "k_xpower_ct"}
+        stage_names = {1: "k_bucket_sort+scan+compact", 2: "k_plane_ct",
+                       4: "k_xpower_tma" if plan.tma else "k_xpower_ct"}
     else:
         stage_bytes = {
             1: lambda k: 16 * N_ATOMS * k + 4 * V * k,             # positions read, grid written

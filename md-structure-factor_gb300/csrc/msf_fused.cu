@@ -1,17 +1,21 @@
 // msf_fused.cu -- the bucketed histogram + FFT chain for power-of-two grids.
 //
 // Per batch of frames (dens.py:277-318 in histogram form):
-//   k_bucket_sort    every block bins its 4096 atoms (exact numpy.histogramdd
+//   k_bucket_sort    every block bins its 2048 atoms (exact numpy.histogramdd
 //                    search), counting-sorts them by x-plane in shared memory
-//                    (lanes of a warp that share a plane merged with
-//                    __match_any_sync) and writes (y*n2 + z, w) entries plus the
-//                    plane offsets of its segment
-//   k_plane_ct       one CTA per (frame, x): the plane's atoms, gathered from
-//                    every segment, are added into the plane in shared memory
-//                    (FP32 atomics on integer weights: exact and independent
-//                    of order); then a two-pass register z-FFT of row pairs
-//                    y = 2p, 2p+1 packed as x[2p] + i x[2p+1], a two-pass
-//                    half-length y-FFT over p, and the 2-D real split
+//                    and writes (y*n2 + z, w) entries plus the plane offsets
+//                    of its segment
+//   k_bucket_scan    plane offsets of the compacted entries (each plane's
+//   k_bucket_compact count padded to even) and every block's segments moved
+//                    to their plane's contiguous range
+//   k_plane_ct       persistent, one plane (frame, x) at a time: the plane's
+//                    atoms, staged by one cp.async.bulk copy under the
+//                    previous plane's FFT, are added into the plane in shared
+//                    memory (FP32 atomics on integer weights: exact and
+//                    independent of order); then a two-pass register z-FFT of
+//                    row pairs y = 2p, 2p+1 packed as x[2p] + i x[2p+1], a
+//                    two-pass half-length y-FFT over p whose second pass is
+//                    fused with the 2-D real split
 //                      E = (W[q,k] + conj W[-q,-k])/2, O = (W[q,k] - conj W[-q,-k])/(2i)
 //                      Y[q,k] = E + w^q O, Y[q+P,k] = E - w^q O   (w = e^{-2 pi i/n1})
 //                    written as the (n1, n2/2+1) half plane.  The density grid
@@ -28,6 +32,7 @@
 #include "msf_bins.cuh"
 #include "msf_ct.cuh"
 #include "msf_r2.cuh"
+#include "msf_tma.cuh"
 
 namespace msf {
 
@@ -42,6 +47,7 @@ struct BucketArgs {
   int* boff;        // (batch, nblk, n0 + 1) per-block plane offsets
   int2* bucket;     // (batch, nblk * kBucketAtoms) entries (y*n2 + z, w)
   int nblk;
+  int* pcount;      // (batch, n0) atoms per plane, summed over the blocks
 };
 
 constexpr int kBucketThreads = 256;
@@ -101,6 +107,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
       hist[idx] = run;                   // becomes the placement cursor
       bo[idx] = run;
       run += loc[j];
+      if (loc[j]) atomicAdd(a.pcount + (int64_t)frame * n0 + idx, loc[j]);
     }
   }
   if (tid == kBucketThreads - 1) bo[n0] = before + incl;
@@ -118,20 +125,20 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
 
 // ----------------------------------------------------------- plane (z, y)
 struct PlaneCtArgs {
-  // bucket source
-  const int* boff;
-  const int2* bucket;
-  int nblk;
   int n0;
   // grid source
   const void* grids;
   int grid_kind;
   int64_t V;
+  // compacted entries: plane x of frame f is pbucket[f * pstride + poff[f][x] ..
+  // poff[f][x + 1]) (an even count)
+  const int2* pbucket;
+  const int* poff;
+  int64_t pstride;
+  int* status;
   // output
   float2* C;
   int64_t Vh;
-  const float2* twz;
-  const float2* twp;
   const float2* twy;
 };
 
@@ -211,9 +218,12 @@ __device__ __forceinline__ void ypass2_split(const float2* buf, float2* out) {
       for (int k2 = 0; k2 < A; ++k2) emit(B * k2, l, a[k2], a[(A - k2) & (A - 1)]);
 #pragma unroll
       for (int k2 = 0; k2 < A; ++k2) emit(B / 2 + B * k2, l, b[k2], b[A - 1 - k2]);
+    } else if (k1 == 0) {            // interior line, k1 = 0: partner (0, -l)
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) emit(B * k2, l, a[k2], b[(A - k2) & (A - 1)]);
     } else {
 #pragma unroll
-      for (int k2 = 0; k2 < A; ++k2) emit(k1 + B * k2, l, a[k2], b[k1 ? A - 1 - k2 : (A - k2) & (A - 1)]);
+      for (int k2 = 0; k2 < A; ++k2) emit(k1 + B * k2, l, a[k2], b[A - 1 - k2]);
       if (u < B) {
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2) emit(k1p + B * k2, l, b[k2], a[A - 1 - k2]);
@@ -273,168 +283,117 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
 }
 
 // Bucket source, persistent: CTA b transforms planes (frame, x) = item b,
-// b + gridDim.x, ... of the batch.  Plane x's atoms sit in one segment per
-// bucketing block; a block scan of the segment lengths (thread t owns
-// segment t) gives the segment tables, and thread t then deposits entries
-// t, t + NT, ... of the concatenated segments.  Before the FFT of plane i,
-// every thread cp.async-copies its own segment of plane i + G to its place in
-// the concatenation (up to kPlanePrefetch*NT entries are staged; the rest are
-// read at deposit time through the tables), and the raw bounds of its
-// segment of plane i + 2G (G = gridDim.x), so their global-memory latency is
-// spent under the FFT instead of between planes.
+// b + gridDim.x, ... of the batch.  A plane's atoms are one contiguous, even
+// range of the compacted entries (k_bucket_compact); thread 0 fetches up to
+// kPlanePrefetch*NT of them into shared memory with one cp.async.bulk copy
+// tracked by an mbarrier, issued before the FFT of the previous plane, so the
+// copy runs under that FFT.  Entries beyond the staged part are read from
+// global memory at deposit time.  The wait is bounded: on timeout the kernel
+// latches MSF_E_TIMEOUT in the plan status word and returns.
 constexpr int kPlanePrefetch = 2;
 
 template <int N1, int N2>
 struct BucketPlaneShape {
   using S = PlaneShape<N1, N2>;
-  static constexpr int NT = S::NT, R = kPlanePrefetch;
-  // plane, segment tables (2 NT + 1 + NT/32 ints, padded to 8 bytes), raw
-  // bounds (NT int2), staged entries (R NT int2)
-  static constexpr size_t TAB_INTS = (2 * NT + 1 + NT / 32 + 1) & ~(size_t)1;
-  static constexpr size_t SMEM = (size_t)N2 * S::SP * sizeof(float2) + TAB_INTS * sizeof(int) +
-                                 (size_t)(NT + R * NT) * sizeof(int2);
+  static constexpr int CAP = kPlanePrefetch * S::NT;   // staged entries (even)
+  // plane (a multiple of 16 bytes), the staged entries, then the mbarrier
+  // and three ints (no static shared memory: the dynamic base keeps its
+  // alignment for the 16-byte stores and the bulk copy)
+  static constexpr size_t SMEM = (size_t)N2 * S::SP * sizeof(float2) + (size_t)CAP * sizeof(int2) + 32;
 };
 
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-               "l"(src)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-               "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 template <int N1, int N2>
 __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtArgs a, int items) {
   using S = PlaneShape<N1, N2>;
-  using BS = BucketPlaneShape<N1, N2>;
-  constexpr int SP = S::SP, NT = S::NT, R = kPlanePrefetch;
-  extern __shared__ float2 smem[];
+  constexpr int SP = S::SP, NT = S::NT, CAP = BucketPlaneShape<N1, N2>::CAP;
+  extern __shared__ __align__(16) float2 smem[];
   float2* buf = smem;                                       // [N2][SP], z major
   float* buff = reinterpret_cast<float*>(buf);
-  int* seg_start = reinterpret_cast<int*>(buf + N2 * SP);   // NT + 1 ints
-  int* seg_lo = seg_start + NT + 1;                         // NT ints
-  int* warp_sum = seg_lo + NT;                              // NT / 32 ints
-  int2* sbounds = reinterpret_cast<int2*>(seg_start + BS::TAB_INTS);   // NT: (bo[x], bo[x + 1])
-  int2* staged = sbounds + NT;                              // R * NT entries
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const bool flat = a.nblk <= NT;
+  int2* staged = reinterpret_cast<int2*>(buf + N2 * SP);    // CAP entries
+  uint64_t* bar = reinterpret_cast<uint64_t*>(staged + CAP);
+  int* ctl = reinterpret_cast<int*>(bar + 1);   // [0] range begin, [1] count, [2] abort flag
+  const int tid = threadIdx.x;
   const int G = gridDim.x;
-  auto has_segment = [&](int item) { return flat && item < items && tid < a.nblk; };
-  auto bounds_ptr = [&](int item) {
+  // thread 0: range (begin, count) of plane `item`, and the copy of its
+  // first CAP entries
+  auto range = [&](int item) {
     const int frame = item / a.n0, x = item - frame * a.n0;
-    return a.boff + ((int64_t)frame * a.nblk + tid) * (a.n0 + 1) + x;
+    const int* po = a.poff + (int64_t)frame * (a.n0 + 1) + x;
+    return make_int2(po[0], po[1] - po[0]);
   };
-  // block scan of the segment lengths into the tables (two barriers);
-  // returns the entry count, `start` gets this thread's segment start
-  auto tables = [&](int lo, int cnt, int& start) {
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane == 31) warp_sum[warp] = incl;
-    __syncthreads();
-    int ws = lane < NT / 32 ? warp_sum[lane] : 0;   // exclusive scan of the warp sums
-#pragma unroll
-    for (int o = 1; o < NT / 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, ws, o);
-      if (lane >= o) ws += y;
-    }
-    const int before = warp ? __shfl_sync(0xffffffffu, ws, warp - 1) : 0;
-    start = before + incl - cnt;
-    seg_start[tid] = start;
-    seg_lo[tid] = lo;
-    if (tid == NT - 1) seg_start[NT] = before + incl;
-    __syncthreads();
-    return seg_start[NT];
+  auto issue = [&](int item, int2 r) {
+    const int ns = r.y < CAP ? r.y : CAP;
+    mbar_expect_tx(bar, (uint32_t)ns * sizeof(int2));
+    if (ns > 0) bulk_load(staged, a.pbucket + (int64_t)(item / a.n0) * a.pstride + r.x, ns * sizeof(int2), bar);
   };
-  auto entry_ptr = [&](int item, int e) {   // needs the tables of `item`
-    int s0 = 0, s1 = a.nblk - 1;            // last segment with seg_start <= e
-    while (s0 < s1) {
-      const int m = (s0 + s1 + 1) >> 1;
-      if (seg_start[m] <= e) s0 = m; else s1 = m - 1;
-    }
-    const int frame = item / a.n0;
-    return a.bucket + ((int64_t)frame * a.nblk + s0) * kBucketAtoms + seg_lo[s0] + (e - seg_start[s0]);
-  };
-  // async copies: thread t copies its own segment of `item` (bounds lo, cnt,
-  // concatenated position start) into the staging area, up to its capacity,
-  // and the raw bounds of its segment of `later`
-  auto stage = [&](int item, int lo, int cnt, int start, int later) {
-    if (cnt > 0) {
-      const int frame = item / a.n0;
-      const int2* src = a.bucket + ((int64_t)frame * a.nblk + tid) * kBucketAtoms + lo;
-      const int n = min(cnt, R * NT - start);
-      for (int j = 0; j < n; ++j) cp_async8(staged + start + j, src + j);
-    }
-    if (has_segment(later)) {
-      const int* bo = bounds_ptr(later);
-      cp_async4(&sbounds[tid].x, bo);
-      cp_async4(&sbounds[tid].y, bo + 1);
-    }
-    cp_async_commit();
-  };
-
+  int2 after = make_int2(0, 0);   // thread 0: range of the plane after the next
   int item = blockIdx.x;
-  int total;
-  {
-    int lo = 0, cnt = 0, start;
-    if (has_segment(item)) {
-      const int* bo = bounds_ptr(item);
-      lo = bo[0];
-      cnt = bo[1] - lo;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    ctl[2] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    int2 r = make_int2(0, 0);
+    if (item < items) {
+      r = range(item);
+      issue(item, r);
     }
-    total = tables(lo, cnt, start);
-    stage(item, lo, cnt, start, item + G);
+    ctl[0] = r.x;
+    ctl[1] = r.y;
+    if (item + G < items) after = range(item + G);
   }
-
+  __syncthreads();
+  uint32_t phase = 0;
   for (; item < items; item += G) {
     const int frame = item / a.n0, x = item - frame * a.n0;
     int4* z4 = reinterpret_cast<int4*>(buf);
     for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
-    cp_async_commit_wait_all();
+    long long spins = 0;
+    while (!mbar_try_wait(bar, phase)) {
+      if (++spins > kWaitLimit) { atomicExch(ctl + 2, 1); break; }
+    }
     __syncthreads();
+    if (ctl[2]) {
+      if (tid == 0) atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
+      break;
+    }
+    phase ^= 1u;
     // integer weights summed in FP32: exact (and order-independent) while a
     // voxel's total stays below 2^24 electrons
-    if (flat) {
-      for (int e = tid; e < total; e += NT) {
-        const int2 v = e < R * NT ? staged[e] : *entry_ptr(item, e);
+    {
+      const int n = ctl[1], ns = n < CAP ? n : CAP;
+      const int2* src = a.pbucket + (int64_t)frame * a.pstride + ctl[0];
+      for (int e = tid; e < n; e += NT) {
+        const int2 v = e < ns ? staged[e] : src[e];
         atomicAdd(buff + pair_offset<N2, SP>(v.x), (float)v.y);
       }
-    } else {
-      // more bucketing blocks than threads: a warp per block, no staging
-      for (int blk = warp; blk < a.nblk; blk += NT / 32) {
-        const int* bo = a.boff + ((int64_t)frame * a.nblk + blk) * (a.n0 + 1);
-        const int e0 = bo[x], e1 = bo[x + 1];
-        const int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
-        for (int e = e0 + lane; e < e1; e += 32) {
-          const int2 v = bk[e];
-          atomicAdd(buff + pair_offset<N2, SP>(v.x), (float)v.y);
-        }
+    }
+    __syncthreads();   // staging area and the range consumed
+    if (tid == 0) {
+      const int next = item + G;
+      if (next < items) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(next, after);
       }
+      ctl[0] = after.x;
+      ctl[1] = after.y;
+      if (next + G < items) after = range(next + G);
     }
-    __syncthreads();
-    // next plane: tables from the staged bounds, then its entries and the
-    // bounds of the plane after it are copied while this plane transforms
-    const int next = item + G;
-    int lo = 0, cnt = 0, start;
-    if (has_segment(next)) {
-      const int2 b = sbounds[tid];
-      lo = b.x;
-      cnt = b.y - b.x;
-    }
-    total = tables(lo, cnt, start);
-    stage(next, lo, cnt, start, next + G);
     plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
     __syncthreads();   // the split has read buf before it is zeroed again
   }
-  cp_async_commit_wait_all();   // no copy left in flight into shared memory at exit
+  // leave no copy in flight into this CTA's shared memory (bounded)
+  if (tid == 0 && ctl[2]) {
+    long long spins = 0;
+    while (!mbar_try_wait(bar, phase) && ++spins < kWaitLimit) {
+    }
+  }
 }
 
 // ------------------------------------------------- x pass + |F|^2 + sum
@@ -497,9 +456,11 @@ __global__ void __launch_bounds__(XShape<N0, W>::NT) k_xpower_ct(XCtArgs a) {
 
 // ---------------------------------------------------------------- dispatch
 template <typename K>
-static void allow_smem_once(K kernel, bool& once) {
+static void allow_smem_once(K kernel, bool& once, size_t bytes = 227 * 1024) {
   if (!once) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    // the exact need: with static shared memory in the kernel, 227 KB of
+    // dynamic shared memory would exceed the per-block limit and be refused
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     // the whole unified L1/shared array as shared memory, so an x-pass CTA
     // finds room beside a plane CTA
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
@@ -513,7 +474,7 @@ static int launch_plane_ct(const PlaneCtArgs& a, int src, int n0, int nframes, c
   static bool once0 = false, once1 = false;
   static int sms = 0;
   if (src == 0) {
-    allow_smem_once(k_plane_ct<N1, N2>, once0);
+    allow_smem_once(k_plane_ct<N1, N2>, once0, BucketPlaneShape<N1, N2>::SMEM);
     if (!sms) {
       int dev = 0;
       cudaGetDevice(&dev);
@@ -523,7 +484,7 @@ static int launch_plane_ct(const PlaneCtArgs& a, int src, int n0, int nframes, c
     const int items = n0 * nframes;
     k_plane_ct<N1, N2><<<items < sms ? items : sms, S::NT, BucketPlaneShape<N1, N2>::SMEM, st>>>(a, items);
   } else {
-    allow_smem_once(k_plane_grid<N1, N2>, once1);
+    allow_smem_once(k_plane_grid<N1, N2>, once1, S::SMEM);
     k_plane_grid<N1, N2><<<dim3(n0, nframes), S::NT, S::SMEM, st>>>(a);
   }
   return launch_status();
@@ -615,12 +576,87 @@ size_t ct_plane_smem(int n1, int n2) {
   return (size_t)n2 * (n1 / 2 + 1) * sizeof(float2) + (size_t)(n2 + n1) * sizeof(float2);
 }
 
+// Plane offsets of the compacted entries (one CTA per frame, thread x per
+// plane): plane x's count (summed over the bucketing blocks by
+// k_bucket_sort, then reset to zero here for the next batch) padded to even
+// with a zero-weight entry, exclusive scan over x -> poff, which also
+// starts the plane's placement cursor.
+__global__ void __launch_bounds__(kMaxN) k_bucket_scan(int* pcount, int n0, int* poff, int* cursor, int2* pbucket,
+                                                      int64_t pstride) {
+  __shared__ int wsum[kMaxN / 32];
+  const int frame = blockIdx.x, x = threadIdx.x;
+  const int lane = x & 31, warp = x >> 5;
+  int tot = 0;
+  if (x < n0) {
+    tot = pcount[(int64_t)frame * n0 + x];
+    pcount[(int64_t)frame * n0 + x] = 0;
+  }
+  const int padded = (tot + 1) & ~1;
+  int incl = padded;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x / 32) ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  if (x >= n0) return;
+  const int base = incl - padded + (warp ? wsum[warp - 1] : 0);
+  int* po = poff + (int64_t)frame * (n0 + 1);
+  po[x] = base;
+  if (x == n0 - 1) po[n0] = base + padded;
+  cursor[(int64_t)frame * n0 + x] = base;
+  if (padded != tot) pbucket[(int64_t)frame * pstride + base + tot] = make_int2(0, 0);
+}
+
+// Every bucketing block's entries moved to their plane's range (one CTA per
+// (block, frame)): each of the block's plane segments reserves its place
+// with one atomic on the plane's cursor (the order of segments within a
+// plane is free: the deposit sums integers exactly); entry e of the block
+// belongs to the last plane x with offset <= e.
+__global__ void __launch_bounds__(kBucketThreads) k_bucket_compact(BucketArgs a, int* cursor, int2* pbucket,
+                                                                   int64_t pstride) {
+  __shared__ int sbo[kMaxN + 1];
+  __shared__ int sdst[kMaxN];
+  const int blk = blockIdx.x, frame = blockIdx.y, n0 = a.d.n0;
+  const int* bo = a.boff + ((int64_t)frame * a.nblk + blk) * (n0 + 1);
+  for (int i = threadIdx.x; i <= n0; i += kBucketThreads) sbo[i] = bo[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < n0; i += kBucketThreads) {
+    const int cnt = sbo[i + 1] - sbo[i];
+    sdst[i] = cnt ? atomicAdd(cursor + (int64_t)frame * n0 + i, cnt) : 0;
+  }
+  __syncthreads();
+  const int total = sbo[n0];
+  const int2* src = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
+  int2* out = pbucket + (int64_t)frame * pstride;
+  for (int e = threadIdx.x; e < total; e += kBucketThreads) {
+    int lo = 0, hi = n0 - 1;
+    while (lo < hi) {
+      const int m = (lo + hi + 1) >> 1;
+      if (sbo[m] <= e) lo = m; else hi = m - 1;
+    }
+    out[sdst[lo] + (e - sbo[lo])] = src[e];
+  }
+}
+
 static BucketArgs bucket_args(const msf_plan* p) {
   BucketArgs b;
   b.d = dep_args(p);
   b.boff = ws_ptr<int>(p, p->off_offsets);
   b.bucket = ws_ptr<int2>(p, p->off_bucket);
   b.nblk = (int)((p->max_atoms + kBucketAtoms - 1) / kBucketAtoms);
+  b.pcount = ws_ptr<int>(p, p->off_pcount);
   return b;
 }
 
@@ -646,6 +682,15 @@ int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weight
     case 3: k_bucket_sort<3><<<grid, kBucketThreads, 0, st>>>(b); break;
     default: k_bucket_sort<4><<<grid, kBucketThreads, 0, st>>>(b); break;
   }
+  int s = launch_status();
+  if (s) return s;
+  int2* pbucket = ws_ptr<int2>(p, p->off_pbucket);
+  int* cursor = ws_ptr<int>(p, p->off_pcursor);
+  k_bucket_scan<<<nframes, ((p->n0 + 31) / 32) * 32, 0, st>>>(b.pcount, p->n0, ws_ptr<int>(p, p->off_poff), cursor,
+                                                          pbucket, p->pstride);
+  s = launch_status();
+  if (s) return s;
+  k_bucket_compact<<<grid, kBucketThreads, 0, st>>>(b, cursor, pbucket, p->pstride);
   return launch_status();
 }
 
@@ -678,17 +723,15 @@ int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int 
 static PlaneCtArgs plane_args(const msf_plan* p) {
   PlaneCtArgs a;
   memset(&a, 0, sizeof(a));
-  a.boff = ws_ptr<int>(p, p->off_offsets);
-  a.bucket = ws_ptr<int2>(p, p->off_bucket);
-  a.nblk = (int)((p->max_atoms + kBucketAtoms - 1) / kBucketAtoms);
-  if (a.nblk < 1) a.nblk = 1;
   a.n0 = p->n0;
   a.V = grid_elems(p);
   a.C = ws_ptr<float2>(p, p->off_cplx);
   a.Vh = half_elems(p);
-  a.twz = ws_ptr<float2>(p, p->off_tw[2]);
-  a.twp = ws_ptr<float2>(p, p->off_twp);
   a.twy = ws_ptr<float2>(p, p->off_tw[1]);
+  a.pbucket = ws_ptr<int2>(p, p->off_pbucket);
+  a.poff = ws_ptr<int>(p, p->off_poff);
+  a.pstride = p->pstride;
+  a.status = ws_ptr<int>(p, p->off_status);
   return a;
 }
 

@@ -58,6 +58,11 @@ struct msf_plan {
   // bucketed chain (variant 3): per-x-plane atom lists
   int64_t max_atoms;
   size_t off_counts, off_offsets, off_cursor, off_bucket;
+  // the entries compacted plane by plane (each plane's range padded to an
+  // even count), the plane offsets, the per-plane counts (kept zero between
+  // batches) and the per-plane placement cursors
+  size_t off_pbucket, off_poff, off_pcount, off_pcursor;
+  int64_t pstride;      // entries per frame in the compacted array
   // TMA tensor maps over the two spectrum buffers for the x pass (CUtensorMap, 128 bytes each)
   alignas(64) unsigned char xtma_map[2][128];
   int xtma_ready;

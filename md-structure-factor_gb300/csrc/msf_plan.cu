@@ -219,6 +219,11 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   p->off_offsets = o; o = align_up(o + (size_t)p->batch * (nblk > 0 ? nblk : 1) * (n[0] + 1) * sizeof(int));
   p->off_cursor = o;
   p->off_bucket = o; o = align_up(o + (size_t)p->batch * nblk * kBucketAtoms * 8);
+  p->pstride = variant == 3 ? ((p->max_atoms + n[0] + 1) & ~(int64_t)1) : 0;
+  p->off_pbucket = o; o = align_up(o + (size_t)p->batch * p->pstride * 8);
+  p->off_poff = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * (n[0] + 1) * sizeof(int) : 0));
+  p->off_pcount = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * n[0] * sizeof(int) : 0));
+  p->off_pcursor = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * n[0] * sizeof(int) : 0));
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
   p->off_cplx2 = o; o = align_up(o + (p->overlap ? (size_t)p->batch * half_elems(p) * sizeof(float2) : 0));
   p->ws_bytes = o;
@@ -263,6 +268,10 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
   if (p->variant != 3) {
     s = cuda_status(cudaMemsetAsync(p->ws + p->off_grid, 0,
                                     (size_t)p->batch * grid_elems(p) * sizeof(int32_t), st));
+    if (s) return s;
+  } else {
+    // per-plane counts start at zero; k_bucket_scan resets them after use
+    s = cuda_status(cudaMemsetAsync(p->ws + p->off_pcount, 0, (size_t)p->batch * p->n0 * sizeof(int), st));
     if (s) return s;
   }
   if (p->overlap && !p->side) {
