@@ -21,11 +21,32 @@
 
 namespace msf {
 
+// L2-coherent loads: the int32 grids are zeroed by the kernel that reads them
 template <int GK>
 __device__ __forceinline__ float load_grid(const void* g, int64_t i) {
-  if (GK == kGridI32) return (float)__ldg(static_cast<const int32_t*>(g) + i);
-  if (GK == kGridF32) return __ldg(static_cast<const float*>(g) + i);
-  return (float)__ldg(static_cast<const double*>(g) + i);
+  if (GK == kGridI32) return (float)__ldcg(static_cast<const int32_t*>(g) + i);
+  if (GK == kGridF32) return __ldcg(static_cast<const float*>(g) + i);
+  return (float)__ldcg(static_cast<const double*>(g) + i);
+}
+
+// Block-strided loop over [0, total) that keeps U global loads in flight per
+// thread: load(e) for U indices first, then store(e, value) for each (a loop
+// that stores after every load waits a full memory latency per element).
+template <int U, typename T, typename L, typename S>
+__device__ __forceinline__ void gather_batched(int total, L load, S store) {
+  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+    T v[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int e = e0 + j * (int)blockDim.x;
+      if (e < total) v[j] = load(e);
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int e = e0 + j * (int)blockDim.x;
+      if (e < total) store(e, v[j]);
+    }
+  }
 }
 
 template <int GK>
@@ -56,7 +77,8 @@ __global__ void __launch_bounds__(512) k_plane(PlaneArgs a) {
   float2* buf = smem;                    // [n2][SP]
   float2* twz = buf + (size_t)n2 * SP;   // n2
   float2* twp = twz + n2;                // P
-  int* posz = reinterpret_cast<int*>(twp + P);
+  float2* twq = twp + P;                 // P: w_{n1}^q, q < P
+  int* posz = reinterpret_cast<int*>(twq + P);
   int* posp = posz + n2;
   const int x = blockIdx.x;
   const int frame = blockIdx.y;
@@ -65,20 +87,25 @@ __global__ void __launch_bounds__(512) k_plane(PlaneArgs a) {
 
   copy_table(twz, a.twz, n2);
   copy_table(twp, a.twp, P);
+  copy_table(twq, a.twy, P);
   copy_table(posz, a.posz, n2);
   copy_table(posp, a.posp, P);
 
   // rows y = 2p, 2p+1 packed as one complex line along z
   void* gw = const_cast<void*>(a.grids);
-  for (int e = threadIdx.x; e < P * n2; e += blockDim.x) {
-    const int p = e / n2;
-    const int z = e - p * n2;
-    const int64_t ia = gbase + (int64_t)(2 * p) * n2 + z;
-    const float va = load_grid<GK>(a.grids, ia);
-    const float vb = load_grid<GK>(a.grids, ia + n2);
-    buf[z * SP + p] = make_float2(va, vb);
-    if (a.zero) { zero_grid<GK>(gw, ia); zero_grid<GK>(gw, ia + n2); }
-  }
+  gather_batched<8, float2>(
+      P * n2,
+      [&](int e) {
+        const int p = e / n2, z = e - p * n2;
+        const int64_t ia = gbase + (int64_t)(2 * p) * n2 + z;
+        const float2 v = make_float2(load_grid<GK>(a.grids, ia), load_grid<GK>(a.grids, ia + n2));
+        if (a.zero) { zero_grid<GK>(gw, ia); zero_grid<GK>(gw, ia + n2); }
+        return v;
+      },
+      [&](int e, float2 v) {
+        const int p = e / n2, z = e - p * n2;
+        buf[z * SP + p] = v;
+      });
   __syncthreads();
   fft_lines(buf, nullptr, a.az, twz, P, SP, 1, true);   // z, lines = pairs
   fft_lines(buf, nullptr, a.ap, twp, n2, 1, SP, false); // half-y, lines = kz positions
@@ -93,7 +120,7 @@ __global__ void __launch_bounds__(512) k_plane(PlaneArgs a) {
     const float2 wm = cconj(buf[posz[kn] * SP + posp[qn]]);
     const float2 E = cscale(cadd(w, wm), 0.5f);
     const float2 O = cscale(cmi(csub(w, wm)), 0.5f);
-    const float2 t = cmul(__ldg(a.twy + q), O);
+    const float2 t = cmul(twq[q], O);
     out[(int64_t)q * nh + k] = cadd(E, t);
     out[(int64_t)(q + P) * nh + k] = csub(E, t);
   }
@@ -127,22 +154,27 @@ __global__ void __launch_bounds__(256) k_zrows(RowsArgs a) {
   copy_table(twz, a.twz, n2);
   copy_table(posz, a.posz, n2);
   void* gw = const_cast<void*>(a.grids);
-  for (int e = threadIdx.x; e < G * n2; e += blockDim.x) {
-    const int g = e / n2;
-    const int z = e - g * n2;
-    const int64_t ra = 2 * (p0 + g);
-    float va = 0.f, vb = 0.f;
-    if (ra < a.rows) {
-      const int64_t ia = frame * a.V + ra * n2 + z;
-      va = load_grid<GK>(a.grids, ia);
-      if (a.zero) zero_grid<GK>(gw, ia);
-      if (ra + 1 < a.rows) {
-        vb = load_grid<GK>(a.grids, ia + n2);
-        if (a.zero) zero_grid<GK>(gw, ia + n2);
-      }
-    }
-    buf[z * S + g] = make_float2(va, vb);
-  }
+  gather_batched<8, float2>(
+      G * n2,
+      [&](int e) {
+        const int g = e / n2, z = e - g * n2;
+        const int64_t ra = 2 * (p0 + g);
+        float va = 0.f, vb = 0.f;
+        if (ra < a.rows) {
+          const int64_t ia = frame * a.V + ra * n2 + z;
+          va = load_grid<GK>(a.grids, ia);
+          if (a.zero) zero_grid<GK>(gw, ia);
+          if (ra + 1 < a.rows) {
+            vb = load_grid<GK>(a.grids, ia + n2);
+            if (a.zero) zero_grid<GK>(gw, ia + n2);
+          }
+        }
+        return make_float2(va, vb);
+      },
+      [&](int e, float2 v) {
+        const int g = e / n2, z = e - g * n2;
+        buf[z * S + g] = v;
+      });
   __syncthreads();
   fft_lines(buf, scratch, a.az, twz, G, S, 1, true);
   float2* out = a.C + frame * a.Vh;
@@ -185,10 +217,13 @@ __global__ void __launch_bounds__(256) k_ycols(ColsArgs a) {
   float2* base = a.C + blockIdx.y * a.Vh + (int64_t)x * n1 * nh + k0;
   copy_table(tw, a.twy, n1);
   copy_table(pos, a.posy, n1);
-  for (int e = threadIdx.x; e < n1 * W; e += blockDim.x) {
-    const int y = e / W, w = e % W;
-    tile[e] = (w < weff) ? base[(int64_t)y * nh + w] : make_float2(0.f, 0.f);
-  }
+  gather_batched<8, float2>(
+      n1 * W,
+      [&](int e) {
+        const int y = e / W, w = e % W;
+        return (w < weff) ? base[(int64_t)y * nh + w] : make_float2(0.f, 0.f);
+      },
+      [&](int e, float2 v) { tile[e] = v; });
   __syncthreads();
   fft_lines(tile, scratch, a.ay, tw, W, W, 1, true);
   for (int e = threadIdx.x; e < n1 * W; e += blockDim.x) {
@@ -233,10 +268,13 @@ __global__ void __launch_bounds__(kXThreads) k_xpower(XArgs a) {
   for (int b = 0; b < a.nframes; ++b) {
     const float2* src = a.C + b * a.Vh + f0;
     __syncthreads();
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      const int x = e / W, w = e % W;
-      tile[e] = (w < weff) ? __ldg(src + (int64_t)x * a.F + w) : make_float2(0.f, 0.f);
-    }
+    gather_batched<8, float2>(
+        nel,
+        [&](int e) {
+          const int x = e / W, w = e % W;
+          return (w < weff) ? __ldg(src + (int64_t)x * a.F + w) : make_float2(0.f, 0.f);
+        },
+        [&](int e, float2 v) { tile[e] = v; });
     __syncthreads();
     fft_lines(tile, scratch, a.ax, tw, W, W, 1, true);
 #pragma unroll

@@ -165,7 +165,9 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
 
   // fused plane variant: n1 even, no generic radix on z or half-y, plane fits
   const int SP = P + ((P & 1) ? 0 : 1);
-  const size_t plane_smem = (size_t)n[2] * SP * sizeof(float2) + (size_t)(n[2] + P) * (sizeof(float2) + sizeof(int));
+  // plane, z and half-y twiddles, w_{n1}^q (q < P), z and half-y positions
+  const size_t plane_smem = (size_t)n[2] * SP * sizeof(float2) + (size_t)(n[2] + 2 * P) * sizeof(float2) +
+                            (size_t)(n[2] + P) * sizeof(int);
   const bool plane_ok = (n[1] % 2 == 0) && P >= 2 && !p->ax[2].generic && !p->axp.generic &&
                         plane_smem <= 220 * 1024;
   const bool fused_ok = ct_plane_ok(n[1], n[2]) && ct_x_width(n[0], d->tile_w) > 0 && n[0] <= kMaxN;
