@@ -68,7 +68,9 @@ typedef struct msf_plan_desc {
   double box[3];          /* box edges L used for binning (mean box when frames are rescaled) */
   int32_t variant;        /* 0 auto, 1 z+y plane from a global grid, 2 split rows/cols,
                              3 bucketed: atoms binned per x-plane and deposited in shared
-                             memory by the plane FFT kernel (power-of-two grids) */
+                             memory by the plane FFT kernel (power-of-two grids),
+                             4 smooth: three sweeps with compile-time mixed-radix FFTs
+                             (every axis 2^a 3^b 5^c in 16..256, or 512) */
   int32_t tile_w;         /* columns per x-pass tile: 0 auto, else 4..32 */
   int32_t rows_per_block; /* row pairs per z-pass block: 0 auto */
   int32_t deposit_block;  /* threads per deposit block: 0 auto */

@@ -21,39 +21,6 @@
 
 namespace msf {
 
-// L2-coherent loads: the int32 grids are zeroed by the kernel that reads them
-template <int GK>
-__device__ __forceinline__ float load_grid(const void* g, int64_t i) {
-  if (GK == kGridI32) return (float)__ldcg(static_cast<const int32_t*>(g) + i);
-  if (GK == kGridF32) return __ldcg(static_cast<const float*>(g) + i);
-  return (float)__ldcg(static_cast<const double*>(g) + i);
-}
-
-// Block-strided loop over [0, total) that keeps U global loads in flight per
-// thread: load(e) for U indices first, then store(e, value) for each (a loop
-// that stores after every load waits a full memory latency per element).
-template <int U, typename T, typename L, typename S>
-__device__ __forceinline__ void gather_batched(int total, L load, S store) {
-  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
-    T v[U];
-#pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int e = e0 + j * (int)blockDim.x;
-      if (e < total) v[j] = load(e);
-    }
-#pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int e = e0 + j * (int)blockDim.x;
-      if (e < total) store(e, v[j]);
-    }
-  }
-}
-
-template <int GK>
-__device__ __forceinline__ void zero_grid(void* g, int64_t i) {
-  if (GK == kGridI32) static_cast<int32_t*>(g)[i] = 0;
-}
-
 struct PlaneArgs {
   const void* grids;
   int64_t V;       // elements per frame grid
@@ -425,6 +392,7 @@ int fft_stage_a(msf_plan* p, const void* grids, int kind, int nframes, int zero,
   if (nframes < 1 || nframes > p->batch) return MSF_E_INVALID;
   // bucketed plans read caller grids with the compile-time plane kernel (never zeroing them)
   if (p->variant == 3) return fused_plane_batch(p, grids, kind, nframes, st);
+  if (p->variant == 4) return smooth_stage_a(p, grids, kind, nframes, zero, st);
   switch (kind) {
     case kGridI32: return stage_a_kind<kGridI32>(p, grids, nframes, zero, st);
     case kGridF32: return stage_a_kind<kGridF32>(p, grids, nframes, zero, st);
@@ -435,6 +403,7 @@ int fft_stage_a(msf_plan* p, const void* grids, int kind, int nframes, int zero,
 int fft_stage_b(msf_plan* p, int nframes, double* sf, cudaStream_t st) {
   if (nframes < 1 || nframes > p->batch) return MSF_E_INVALID;
   if (p->variant == 3) return fused_x_batch(p, nframes, sf, st);
+  if (p->variant == 4) return smooth_stage_b(p, nframes, sf, st);
   return launch_xpower(p, nframes, sf, st);
 }
 

@@ -87,24 +87,24 @@ inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? MSF_OK : MSF_E
 inline int launch_status() { return cuda_status(cudaGetLastError()); }
 
 // ---------------------------------------------------------------- complex
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 // multiply by -i
-__device__ __forceinline__ float2 cmi(float2 a) { return make_float2(a.y, -a.x); }
+__host__ __device__ __forceinline__ float2 cmi(float2 a) { return make_float2(a.y, -a.x); }
 // multiply by +i
-__device__ __forceinline__ float2 cpi(float2 a) { return make_float2(-a.y, a.x); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cpi(float2 a) { return make_float2(-a.y, a.x); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
 // Forward DFT butterflies (kernel e^{-2 pi i jk/R}) on R values in registers.
 // Constants are cos/sin of 2 pi/R and 4 pi/5 rounded to float.
 template <int R> struct Bfly;
 
 template <> struct Bfly<2> {
-  static __device__ __forceinline__ void run(float2* a) {
+  static __host__ __device__ __forceinline__ void run(float2* a) {
     float2 t = a[1];
     a[1] = csub(a[0], t);
     a[0] = cadd(a[0], t);
@@ -112,7 +112,7 @@ template <> struct Bfly<2> {
 };
 
 template <> struct Bfly<3> {
-  static __device__ __forceinline__ void run(float2* a) {
+  static __host__ __device__ __forceinline__ void run(float2* a) {
     const float s3 = 0.866025403784438647f;  // sin(2 pi/3)
     float2 t = cadd(a[1], a[2]);
     float2 u = csub(a[1], a[2]);
@@ -126,7 +126,7 @@ template <> struct Bfly<3> {
 };
 
 template <> struct Bfly<4> {
-  static __device__ __forceinline__ void run(float2* a) {
+  static __host__ __device__ __forceinline__ void run(float2* a) {
     float2 t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
     float2 t2 = cadd(a[1], a[3]), t3 = cmi(csub(a[1], a[3]));
     a[0] = cadd(t0, t2);
@@ -137,7 +137,7 @@ template <> struct Bfly<4> {
 };
 
 template <> struct Bfly<5> {
-  static __device__ __forceinline__ void run(float2* a) {
+  static __host__ __device__ __forceinline__ void run(float2* a) {
     const float c1 = 0.309016994374947424f;   // cos(2 pi/5)
     const float c2 = -0.809016994374947424f;  // cos(4 pi/5)
     const float s1 = 0.951056516295153572f;   // sin(2 pi/5)
@@ -158,7 +158,7 @@ template <> struct Bfly<5> {
 };
 
 template <> struct Bfly<8> {
-  static __device__ __forceinline__ void run(float2* a) {
+  static __host__ __device__ __forceinline__ void run(float2* a) {
     const float h = 0.707106781186547524f;  // 1/sqrt(2)
     float2 e[4] = {a[0], a[2], a[4], a[6]};
     float2 o[4] = {a[1], a[3], a[5], a[7]};
@@ -289,6 +289,10 @@ int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, i
 void plan_release(msf_plan* p);
 // x pass with TMA tile loads (msf_xtma.cu); prepared at bind time
 int plane_twiddles_init();               // constant-memory twiddles of the plane kernel, once per device
+// smooth variant (msf_smooth.cu): axes 2^a 3^b 5^c in 16..256, or 512
+bool smooth_ok(int n);
+int smooth_stage_a(const msf_plan* p, const void* grids, int grid_kind, int nframes, int zero, cudaStream_t st);
+int smooth_stage_b(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
 bool xtma_ok(int n0, int w);
 int xtma_prepare(msf_plan* p);
 int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf);
@@ -312,5 +316,38 @@ enum PosLayout { kLayoutF32x4 = 0, kLayoutF64 = 1, kLayoutF32xyz = 2 };
 
 // grid kinds for fft_power_batch
 enum GridKind { kGridI32 = 0, kGridF32 = 1, kGridF64 = 2 };
+
+// L2-coherent loads: the int32 grids are zeroed by the kernel that reads them
+template <int GK>
+__device__ __forceinline__ float load_grid(const void* g, int64_t i) {
+  if (GK == kGridI32) return (float)__ldcg(static_cast<const int32_t*>(g) + i);
+  if (GK == kGridF32) return __ldcg(static_cast<const float*>(g) + i);
+  return (float)__ldcg(static_cast<const double*>(g) + i);
+}
+
+// Block-strided loop over [0, total) that keeps U global loads in flight per
+// thread: load(e) for U indices first, then store(e, value) for each (a loop
+// that stores after every load waits a full memory latency per element).
+template <int U, typename T, typename L, typename S>
+__device__ __forceinline__ void gather_batched(int total, L load, S store) {
+  for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+    T v[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int e = e0 + j * (int)blockDim.x;
+      if (e < total) v[j] = load(e);
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int e = e0 + j * (int)blockDim.x;
+      if (e < total) store(e, v[j]);
+    }
+  }
+}
+
+template <int GK>
+__device__ __forceinline__ void zero_grid(void* g, int64_t i) {
+  if (GK == kGridI32) static_cast<int32_t*>(g)[i] = 0;
+}
 
 }  // namespace msf

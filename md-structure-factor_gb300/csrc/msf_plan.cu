@@ -150,7 +150,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   for (int i = 0; i < 3; ++i)
     if (!(d->box[i] > 0.0) || !isfinite(d->box[i])) return MSF_E_INVALID;
   if (d->batch < 0 || d->batch > 256) return MSF_E_INVALID;
-  if (d->variant < 0 || d->variant > 3) return MSF_E_INVALID;
+  if (d->variant < 0 || d->variant > 4) return MSF_E_INVALID;
   if (d->max_atoms < 0 || (d->options & ~MSF_PLAN_NO_OVERLAP)) return MSF_E_INVALID;
   if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
@@ -171,10 +171,12 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   const bool plane_ok = (n[1] % 2 == 0) && P >= 2 && !p->ax[2].generic && !p->axp.generic &&
                         plane_smem <= 220 * 1024;
   const bool fused_ok = ct_plane_ok(n[1], n[2]) && ct_x_width(n[0], d->tile_w) > 0 && n[0] <= kMaxN;
+  const bool smooth = smooth_ok(n[0]) && smooth_ok(n[1]) && smooth_ok(n[2]);
   int variant = d->variant;
-  if (variant == 0) variant = fused_ok ? 3 : (plane_ok ? 1 : 2);
+  if (variant == 0) variant = fused_ok ? 3 : (smooth ? 4 : (plane_ok ? 1 : 2));
   if (variant == 1 && !plane_ok) return MSF_E_UNSUPPORTED;
   if (variant == 3 && !fused_ok) return MSF_E_UNSUPPORTED;
+  if (variant == 4 && !smooth) return MSF_E_UNSUPPORTED;
   p->max_atoms = d->max_atoms;
   p->overlap = variant == 3 && !(d->options & MSF_PLAN_NO_OVERLAP);
   p->variant = variant;

@@ -92,7 +92,7 @@ __host__ __device__ constexpr float2 w64(int k) {
 
 // w_R^m for R dividing 64
 template <int R>
-__device__ __forceinline__ float2 wr(int m) { return w64((m % R) * (64 / R)); }
+__host__ __device__ __forceinline__ float2 wr(int m) { return w64((m % R) * (64 / R)); }
 
 template <int R> struct Split {
   static constexpr int A = (R == 16) ? 4 : ((R == 32) ? 4 : 8);   // R = A * B
@@ -100,7 +100,7 @@ template <int R> struct Split {
 };
 
 template <int R>
-__device__ __forceinline__ void reg_dft(float2* a) {
+__host__ __device__ __forceinline__ void reg_dft(float2* a) {
   if constexpr (R == 1) {
   } else if constexpr (R <= 8 && R != 6) {
     Bfly<R>::run(a);

@@ -1,0 +1,298 @@
+// msf_smooth.cu -- three-sweep R2C 3-D FFT with |F|^2 and the frame sum for
+// grids whose axes are all 2^a 3^b 5^c lengths from 16 to 256, or 512
+// (variant 4, "smooth"): the batched multi-system workload of uneven grid
+// shapes and the 512^3 stress grid.  Replaces dens.py:313-318 as msf_fft.cu
+// does, with every axis length a compile-time constant and every line
+// transformed by the two-pass mixed-radix register FFT of msf_mixed.cuh
+// (one exchange through shared memory per pass) instead of one pass per
+// radix stage with runtime index arithmetic.
+//
+//   k_zs<n2>  G row pairs (y = 2p, 2p+1 of the flattened (x, y) rows) per CTA,
+//             read from the int32 grid (which is zeroed behind the read) as
+//             x[2p] + i x[2p+1], z-FFT, split into the two rows' half spectra
+//   k_ys<n1>  (x, W kz columns) per CTA: y-FFT in place in the spectra
+//   k_xs<n0>  W (y, kz) columns per CTA: x-FFT of every frame of the batch,
+//             |F|^2 summed in FP32 in registers, one FP64 RMW of sf
+#include "msf_mixed.cuh"
+
+namespace msf {
+
+namespace {
+
+constexpr int kSmoothThreads = 256;
+constexpr int kSmoothW = 16;   // columns per CTA of the y and x sweeps
+
+__host__ __device__ constexpr int smooth_rows(int n2) {
+  // row pairs per z CTA: N2 * G <= 8192 complex, G a power of two <= 64
+  return n2 <= 128 ? 64 : (n2 <= 256 ? 32 : 16);
+}
+
+struct SmZArgs {
+  const void* grids;
+  int kind;         // GridKind of `grids`
+  int64_t V;        // elements per frame grid
+  float2* C;
+  int64_t Vh;       // complex elements per frame half spectrum
+  int64_t rows;     // n0 * n1 rows per frame
+  int zero;
+  const float2* tw; // w_n2^k
+};
+
+__device__ __forceinline__ float load_any(const void* g, int kind, int64_t i) {
+  if (kind == kGridI32) return load_grid<kGridI32>(g, i);
+  if (kind == kGridF32) return load_grid<kGridF32>(g, i);
+  return load_grid<kGridF64>(g, i);
+}
+
+template <int N2>
+__global__ void __launch_bounds__(kSmoothThreads) k_zs(SmZArgs a) {
+  constexpr int G = smooth_rows(N2), S = G + 1, NH = N2 / 2 + 1, NT = kSmoothThreads;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* buf = smem;              // [N2][S]: sample z of line g at buf[z*S + g]
+  float2* tw = buf + N2 * S;       // N2
+  const int frame = blockIdx.y;
+  const int64_t p0 = (int64_t)blockIdx.x * G;
+  copy_table(tw, a.tw, N2);
+  void* gw = const_cast<void*>(a.grids);
+  gather_batched<8, float2>(
+      G * N2,
+      [&](int e) {
+        const int g = e / N2, z = e - g * N2;
+        const int64_t ra = 2 * (p0 + g);
+        float va = 0.f, vb = 0.f;
+        if (ra < a.rows) {
+          const int64_t ia = frame * a.V + ra * N2 + z;
+          va = load_any(a.grids, a.kind, ia);
+          if (a.zero) zero_grid<kGridI32>(gw, ia);
+          if (ra + 1 < a.rows) {
+            vb = load_any(a.grids, a.kind, ia + N2);
+            if (a.zero) zero_grid<kGridI32>(gw, ia + N2);
+          }
+        }
+        return make_float2(va, vb);
+      },
+      [&](int e, float2 v) {
+        const int g = e / N2, z = e - g * N2;
+        buf[z * S + g] = v;
+      });
+  __syncthreads();
+  mixed::fft2_lines<N2, G, S, 1, NT>(buf, tw);
+  // rows 2p and 2p+1 from the packed line: (P[k] + conj P[-k]) / 2 and
+  // (P[k] - conj P[-k]) / (2i)
+  float2* out = a.C + frame * a.Vh;
+  for (int e = threadIdx.x; e < G * NH; e += NT) {
+    const int g = e / NH, k = e - g * NH;
+    const int64_t ra = 2 * (p0 + g);
+    if (ra >= a.rows) continue;
+    const float2 P = buf[k * S + g];
+    const float2 Q = cconj(buf[((N2 - k) % N2) * S + g]);
+    out[ra * NH + k] = cscale(cadd(P, Q), 0.5f);
+    if (ra + 1 < a.rows) out[(ra + 1) * NH + k] = cscale(cmi(csub(P, Q)), 0.5f);
+  }
+}
+
+struct SmYArgs {
+  float2* C;
+  int64_t Vh;
+  int nh;
+  const float2* tw; // w_n1^k
+};
+
+template <int N1>
+__global__ void __launch_bounds__(kSmoothThreads) k_ys(SmYArgs a) {
+  constexpr int W = kSmoothW, NT = kSmoothThreads;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tile = smem;             // [N1][W]
+  float2* tw = tile + N1 * W;      // N1
+  const int nh = a.nh;
+  const int ntile = (nh + W - 1) / W;
+  const int x = blockIdx.x / ntile;
+  const int k0 = (blockIdx.x - x * ntile) * W;
+  const int weff = min(W, nh - k0);
+  float2* base = a.C + blockIdx.y * a.Vh + (int64_t)x * N1 * nh + k0;
+  copy_table(tw, a.tw, N1);
+  gather_batched<8, float2>(
+      N1 * W,
+      [&](int e) {
+        const int y = e / W, w = e % W;
+        return w < weff ? base[(int64_t)y * nh + w] : make_float2(0.f, 0.f);
+      },
+      [&](int e, float2 v) { tile[e] = v; });
+  __syncthreads();
+  mixed::fft2_lines<N1, W, W, 1, NT>(tile, tw);
+  for (int e = threadIdx.x; e < N1 * W; e += NT) {
+    const int y = e / W, w = e % W;
+    if (w < weff) base[(int64_t)y * nh + w] = tile[e];
+  }
+}
+
+struct SmXArgs {
+  const float2* C;
+  int64_t Vh;
+  int nframes;
+  double* sf;
+  int64_t F;        // n1 * nh columns
+  const float2* tw; // w_n0^k
+};
+
+template <int N0>
+__global__ void __launch_bounds__(kSmoothThreads) k_xs(SmXArgs a) {
+  constexpr int W = kSmoothW, NT = kSmoothThreads;
+  constexpr int A = mixed::Split2m<N0>::A, B = mixed::Split2m<N0>::B;
+  constexpr int I2 = B * W, PER = (I2 + NT - 1) / NT;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* tile = smem;             // [N0][W]
+  float2* tw = tile + N0 * W;      // N0
+  const int64_t f0 = (int64_t)blockIdx.x * W;
+  const int weff = (int)min((int64_t)W, a.F - f0);
+  copy_table(tw, a.tw, N0);
+  // pass-2 items (k1, column l) owned by this thread: X[k1 + B k2] in acc
+  float acc[PER][A];
+#pragma unroll
+  for (int j = 0; j < PER; ++j)
+#pragma unroll
+    for (int k = 0; k < A; ++k) acc[j][k] = 0.f;
+  for (int b = 0; b < a.nframes; ++b) {
+    const float2* src = a.C + b * a.Vh + f0;
+    __syncthreads();   // the previous frame's pass 2 is done with the tile
+    gather_batched<8, float2>(
+        N0 * W,
+        [&](int e) {
+          const int x = e / W, w = e % W;
+          return w < weff ? __ldg(src + (int64_t)x * a.F + w) : make_float2(0.f, 0.f);
+        },
+        [&](int e, float2 v) { tile[e] = v; });
+    __syncthreads();
+    mixed::pass1<N0, W, W, 1, NT>(tile, tw);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int it = j * NT + threadIdx.x;
+      if (I2 % NT == 0 || it < I2) {
+        const int l = it % W, k1 = it / W;
+        float2 r[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) r[n1] = tile[(A * k1 + n1) * W + l];
+        mixed::reg_dftm<A>(r);
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = fmaf(r[k2].x, r[k2].x, fmaf(r[k2].y, r[k2].y, acc[j][k2]));
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int it = j * NT + threadIdx.x;
+    const int l = it % W, k1 = it / W;
+    if ((I2 % NT == 0 || it < I2) && l < weff) {
+      double* d = a.sf + (int64_t)k1 * a.F + f0 + l;
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) {
+        double* dk = d + (int64_t)B * k2 * a.F;
+        *dk = *dk + (double)acc[j][k2];
+      }
+    }
+  }
+}
+
+template <typename K>
+void allow_smem_once(K kernel, bool& once, size_t bytes) {
+  if (!once) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    once = true;
+  }
+}
+
+template <int N2>
+int launch_zs(const msf_plan* p, const void* grids, int kind, int nframes, int zero, cudaStream_t st) {
+  constexpr int G = smooth_rows(N2);
+  const size_t smem = ((size_t)N2 * (G + 1) + N2) * sizeof(float2);
+  static bool once = false;
+  allow_smem_once(k_zs<N2>, once, smem);
+  SmZArgs a;
+  a.grids = grids;
+  a.kind = kind;
+  a.V = grid_elems(p);
+  a.C = ws_ptr<float2>(p, p->off_cplx);
+  a.Vh = half_elems(p);
+  a.rows = (int64_t)p->n0 * p->n1;
+  a.zero = kind == kGridI32 ? zero : 0;   // caller float grids are never zeroed
+  a.tw = ws_ptr<float2>(p, p->off_tw[2]);
+  const int64_t pairs = (a.rows + 1) / 2;
+  k_zs<N2><<<dim3((unsigned)((pairs + G - 1) / G), nframes), kSmoothThreads, smem, st>>>(a);
+  return launch_status();
+}
+
+template <int N1>
+int launch_ys(const msf_plan* p, int nframes, cudaStream_t st) {
+  const size_t smem = ((size_t)N1 * kSmoothW + N1) * sizeof(float2);
+  static bool once = false;
+  allow_smem_once(k_ys<N1>, once, smem);
+  SmYArgs a;
+  a.C = ws_ptr<float2>(p, p->off_cplx);
+  a.Vh = half_elems(p);
+  a.nh = p->nh;
+  a.tw = ws_ptr<float2>(p, p->off_tw[1]);
+  const int ntile = (p->nh + kSmoothW - 1) / kSmoothW;
+  k_ys<N1><<<dim3(p->n0 * ntile, nframes), kSmoothThreads, smem, st>>>(a);
+  return launch_status();
+}
+
+template <int N0>
+int launch_xs(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
+  const size_t smem = ((size_t)N0 * kSmoothW + N0) * sizeof(float2);
+  static bool once = false;
+  allow_smem_once(k_xs<N0>, once, smem);
+  SmXArgs a;
+  a.C = ws_ptr<float2>(p, p->off_cplx);
+  a.Vh = half_elems(p);
+  a.nframes = nframes;
+  a.sf = sf;
+  a.F = (int64_t)p->n1 * p->nh;
+  a.tw = ws_ptr<float2>(p, p->off_tw[0]);
+  k_xs<N0><<<(unsigned)((a.F + kSmoothW - 1) / kSmoothW), kSmoothThreads, smem, st>>>(a);
+  return launch_status();
+}
+
+int zs_dispatch(const msf_plan* p, const void* grids, int kind, int nframes, int zero, cudaStream_t st) {
+  switch (p->n2) {
+#define X(N) case N: return launch_zs<N>(p, grids, kind, nframes, zero, st);
+    MSF_SMOOTH_SIZES(X)
+#undef X
+  }
+  return MSF_E_UNSUPPORTED;
+}
+
+}  // namespace
+
+bool smooth_ok(int n) {
+  switch (n) {
+#define X(N) case N: return true;
+    MSF_SMOOTH_SIZES(X)
+#undef X
+  }
+  return false;
+}
+
+// z and y sweeps: grids (int32 / float32 / float64, frame-major) -> spectra
+int smooth_stage_a(const msf_plan* p, const void* grids, int grid_kind, int nframes, int zero, cudaStream_t st) {
+  const int s = zs_dispatch(p, grids, grid_kind, nframes, zero, st);
+  if (s) return s;
+  switch (p->n1) {
+#define X(N) case N: return launch_ys<N>(p, nframes, st);
+    MSF_SMOOTH_SIZES(X)
+#undef X
+  }
+  return MSF_E_UNSUPPORTED;
+}
+
+// x sweep + |F|^2 + FP64 frame sum
+int smooth_stage_b(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
+  switch (p->n0) {
+#define X(N) case N: return launch_xs<N>(p, nframes, sf, st);
+    MSF_SMOOTH_SIZES(X)
+#undef X
+  }
+  return MSF_E_UNSUPPORTED;
+}
+
+}  // namespace msf

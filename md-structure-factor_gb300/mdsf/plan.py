@@ -16,7 +16,7 @@ import torch
 from . import _lib
 from ._lib import c_p, call, load
 
-VARIANTS = {0: "auto", 1: "plane", 2: "split", 3: "bucketed"}
+VARIANTS = {0: "auto", 1: "plane", 2: "split", 3: "bucketed", 4: "smooth"}
 
 
 def stream_ptr(device=None):

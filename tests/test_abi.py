@@ -54,7 +54,7 @@ def create(**kw):
 
 @pytest.mark.parametrize("kw,code", [
     (dict(dims=(1, 64, 64)), -2), (dict(dims=(64, 2048, 64)), -2), (dict(box=(0.0, 1, 1)), -1),
-    (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=4), -1),
+    (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=5), -1),
     (dict(tile_w=12), -1), (dict(deposit_block=100), -1), (dict(max_atoms=-1), -1),
     (dict(dims=(48, 48, 48), variant=3), -2),
 ])
@@ -90,7 +90,8 @@ def test_plan_layout_and_query():
 
 def test_split_variant_for_odd_and_prime_sizes():
     lib = mdsf.load()
-    for dims, variant in (((75, 81, 48), 2), ((64, 74, 26), 2), ((48, 48, 48), 1), ((512, 512, 512), 2)):
+    for dims, variant in (((75, 81, 48), 4), ((64, 74, 26), 2), ((48, 48, 48), 4), ((512, 512, 512), 4),
+                          ((48, 48, 14), 2), ((1024, 16, 16), 1)):
         st, h = create(dims=dims)
         assert st == 0
         q = (C.c_int32 * 8)()

@@ -2,7 +2,8 @@
 
 Bar: max |S - S_ref| <= 1e-5 * max(S_ref) for every size class: powers of
 two, 2^a 3^b 5^c (batched-system sizes), odd last axes, sizes with a prime
-factor > 5 (generic radix), both FFT variants."""
+factor > 5 (generic radix), the plane, split and smooth (compile-time
+mixed-radix) variants."""
 import numpy as np
 import pytest
 import torch
@@ -15,7 +16,7 @@ TOL = 1e-5
 
 SHAPES = [(64, 64, 64), (256, 256, 128), (48, 50, 54), (75, 81, 125), (96, 100, 243), (64, 74, 26),
           (14, 22, 38), (2, 4, 2), (3, 5, 7), (128, 96, 160), (512, 8, 16), (8, 512, 16), (16, 8, 512),
-          (200, 216, 240)]
+          (200, 216, 240), (512, 18, 20), (24, 512, 25), (30, 27, 512), (250, 162, 45)]
 
 
 def grids_for(shape, n, seed, kind="int"):
@@ -44,7 +45,7 @@ def test_power_accum_int_grids(shape):
 
 
 @pytest.mark.parametrize("shape", [(64, 64, 64), (48, 60, 80), (256, 256, 128)])
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 4])
 @pytest.mark.parametrize("tile_w", [4, 8, 16])
 def test_variants_and_tiles_agree(shape, variant, tile_w):
     g = grids_for(shape, 2, 7)
