@@ -173,6 +173,29 @@ def run_reference(args):
     return 0
 
 
+def run_batched_only(torch, dev, args):
+    """The batched-systems workload alone (for launch lists and ncu captures)."""
+    from mdsf.batch import BatchedSystems, random_batch
+    systems = random_batch(64, seed=5, device=dev)
+    frames = sum(int(s["pos_w"].shape[0]) for s in systems)
+    b = BatchedSystems(systems, n_streams=8, device=dev)
+    for _ in range(2):
+        b.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        b.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    variants = [b.tuning(i)["variant"] for i in range(len(systems))]
+    print(json.dumps({"metric": "batched systems frames/s (64 uneven systems, one graph)",
+                      "value": frames / (ms / 1000.0), "unit": "frames/s", "frames_per_run": frames,
+                      "ms_per_run": ms, "variants": {str(v): variants.count(v) for v in sorted(set(variants))}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -185,6 +208,8 @@ def main():
     ap.add_argument("--no-overlap", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="only the 64 uneven batched systems (one graph, 2 warm-up + `--steps` replays)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -204,6 +229,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.batched_only:
+        return run_batched_only(torch, dev, args)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
@@ -470,9 +497,10 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / 2
     out["batched_systems_frames_per_s"] = frames / (ms / 1000.0)
+    variants = [b.tuning(i)["variant"] for i in range(64)]
     out["batched_systems_note"] = (f"64 systems, {frames} frames, one graph launch per run "
-                                   f"({sum(1 for i in range(64) if b.tuning(i)['variant'] == 3)} on the bucketed "
-                                   "power-of-two path)")
+                                   f"({variants.count(3)} on the bucketed power-of-two chain, "
+                                   f"{variants.count(4)} on the smooth mixed-radix chain)")
     del b, systems
     torch.cuda.empty_cache()
     return out
