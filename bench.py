@@ -208,6 +208,8 @@ def main():
     ap.add_argument("--no-overlap", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--stream-chunk", type=int, default=0,
+                    help="frames per host->device chunk of the e2e path (0: the API default, one batch)")
     ap.add_argument("--batched-only", action="store_true",
                     help="only the 64 uneven batched systems (one graph, 2 warm-up + `--steps` replays)")
     args = ap.parse_args()
@@ -321,7 +323,8 @@ def main():
     sf_h = torch.empty(plan.half_shape, dtype=torch.float64).pin_memory()
 
     def e2e_step():
-        out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning, stream_chunk=plan.batch * 4)
+        out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning,
+                                    stream_chunk=args.stream_chunk or None)
         if world > 1:
             dist.all_reduce(out)
         sf_h.copy_(out, non_blocking=True)

@@ -132,7 +132,7 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
                 raise ValueError("weights must have one entry per atom")
         wptr = wd.data_ptr() if wd is not None else 0
         scp = sc.data_ptr() if sc is not None else 0
-        chunk = int(stream_chunk or 4 * plan.batch)
+        chunk = int(stream_chunk or plan.batch)   # one batch: the first copy hides soonest
         if not host or T <= chunk or N == 0:
             p = to_device(pos, device, tdt)
             _launch_chain(plan, code, p.data_ptr(), wptr, N, T, scp, flags, sf, st)
