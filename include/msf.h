@@ -46,7 +46,12 @@ enum {
 /* Flags for the deposit / chain calls. */
 enum {
   MSF_WRAP = 1,          /* periodic wrap r<L?r:r-L; r>0?r:r+L first (dens.py:204-212) */
-  MSF_NO_ZERO_SF = 0     /* (default) accumulate into sf */
+  MSF_NO_ZERO_SF = 0,    /* (default) accumulate into sf */
+  MSF_CONTINUE = 2       /* msf_hist_sf_* only: more calls on this plan, stream and sf
+                            follow (e.g. chunks streamed from the host).  A bucketed plan
+                            keeps its x pass overlapping across the calls and leaves the
+                            last one running on its side stream; sf is complete on
+                            `stream` only after a later call without this flag. */
 };
 
 const char* msf_strerror(int status);

@@ -111,6 +111,9 @@ int hist_deposit_batch(const msf_plan* p, const void* pos, const int32_t* weight
 using namespace msf;
 
 static int check_flags(int flags) { return (flags & ~MSF_WRAP) ? MSF_E_INVALID : MSF_OK; }
+static int check_chain_flags(int flags) {
+  return (flags & ~(MSF_WRAP | MSF_CONTINUE)) ? MSF_E_INVALID : MSF_OK;
+}
 
 extern "C" {
 
@@ -150,20 +153,24 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
   if (n_atoms > 0 && n_frames > 0 && (!pos || (layout != kLayoutF32x4 && !weights)))
     return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
-  if (check_flags(flags)) return MSF_E_INVALID;
+  if (check_chain_flags(flags)) return MSF_E_INVALID;
+  const bool cont = flags & MSF_CONTINUE;
+  flags &= ~MSF_CONTINUE;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
   const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
   const size_t esize = layout == kLayoutF32x4 ? 4 * sizeof(float)
                        : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
   if (p->variant == 3 && n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
-  if (p->variant == 3 && p->overlap && n_frames > p->batch) {
+  if (p->variant == 3 && p->overlap && (n_frames > p->batch || cont || p->chain_k > 0)) {
     // batch b: bucket sort + plane FFT into spectrum buffer b%2 on `st`, the
     // x pass of batch b on `side` (after that plane FFT), overlapping the
     // plane FFT of batch b+1; the plane FFT of batch b+2 waits for the x pass
-    // of batch b before reusing its buffer; `st` finally joins `side`.
+    // of batch b before reusing its buffer; `st` finally joins `side`.  With
+    // MSF_CONTINUE the batch count carries over to the next call and the
+    // join is left to the call that ends the chain.
     int s = MSF_OK;
-    int64_t k = 0;
+    int64_t k = p->chain_k;
     for (int64_t f = 0; f < n_frames && !s; f += p->batch, ++k) {
       const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
       const int buf = (int)(k & 1);
@@ -177,6 +184,11 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
       if (!s) s = fused_x_batch(p, nb, sf, p->side, buf);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_x[buf], p->side));
     }
+    if (cont && !s) {
+      p->chain_k = k;
+      return MSF_OK;
+    }
+    p->chain_k = 0;
     // join: every x pass (recorded in order on `side`) precedes the last event
     if (k >= 1 && !s) s = cuda_status(cudaStreamWaitEvent(st, p->ev_x[(k - 1) & 1], 0));
     return s;

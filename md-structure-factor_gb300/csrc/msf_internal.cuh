@@ -73,6 +73,9 @@ struct msf_plan {
   size_t off_cplx2;
   cudaStream_t side;
   cudaEvent_t ev_plane[2], ev_x[2];
+  // a chain continued over several calls (MSF_CONTINUE): batches issued so
+  // far, for the spectrum-buffer parity and the reuse waits; 0 when joined
+  int64_t chain_k;
 };
 
 namespace msf {

@@ -291,6 +291,7 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
   }
   s = xtma_prepare(p);
   if (s) return s;
+  p->chain_k = 0;
   p->bound = 1;
   return MSF_OK;
 }

@@ -21,6 +21,7 @@ c_d = C.c_double
 c_size = C.c_size_t
 
 MSF_WRAP = 1
+MSF_CONTINUE = 2
 ERRORS = {
     0: "MSF_OK", -1: "MSF_E_INVALID", -2: "MSF_E_UNSUPPORTED", -3: "MSF_E_WORKSPACE",
     -4: "MSF_E_CUDA", -5: "MSF_E_RANGE", -6: "MSF_E_NOT_BOUND", -7: "MSF_E_TIMEOUT",

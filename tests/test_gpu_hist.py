@@ -127,3 +127,37 @@ def test_large_grid_512_cubed():
     ref = ohist.hist_sf(pos, box, w, (512, 512, 512))
     got = mdsf.structure_factor(pos, box, w, (512, 512, 512), tuning=dict(batch=1)).cpu().numpy()
     assert rel_err(got, ref) < TOL
+
+
+@pytest.mark.parametrize("chunk", [3, 4, 8])
+def test_host_streamed_chunks(chunk):
+    """Host positions streamed to the device in chunks (double-buffered on a
+    side stream, one chain call per chunk, uneven last chunk) equal the
+    oracle."""
+    pos, box, w = synth.uniform_system(4000, (2.0, 2.2, 1.8), frames=23, seed=31)
+    ref = ohist.hist_sf(pos, box, w, (64, 64, 32))
+    got = mdsf.structure_factor(pos.astype(np.float32), box, w, (64, 64, 32),
+                                tuning=dict(batch=4), stream_chunk=chunk).cpu().numpy()
+    assert mdsf.get_plan((64, 64, 32), box, max_atoms=4000, batch=4).tuning()["variant"] == "bucketed"
+    assert rel_err(got, ref) < TOL
+
+
+def test_continue_flag_equals_one_call():
+    """Three calls (MSF_CONTINUE, MSF_CONTINUE, plain) on one plan and sf give
+    the same sf as one call over all frames, bit for bit (chunks on batch
+    boundaries, so the FP32 batch sums are the same)."""
+    from mdsf._lib import MSF_CONTINUE, c_p, call
+    pos, box, w = synth.uniform_system(3000, (2.0, 2.0, 2.0), frames=11, seed=5)
+    p4 = torch.from_numpy(synth.pack_float4(pos.astype(np.float32), w)).cuda()
+    plan = mdsf.get_plan((64, 64, 64), box, max_atoms=3000, batch=2, variant=3)
+    st = c_p(torch.cuda.current_stream().cuda_stream)
+    one = torch.zeros(plan.half_shape, dtype=torch.float64, device="cuda")
+    call("msf_hist_sf_f32", plan.handle, c_p(p4.data_ptr()), 3000, 11, c_p(0), 0, c_p(one.data_ptr()), st)
+    three = torch.zeros_like(one)
+    for f0, f1, fl in ((0, 4, MSF_CONTINUE), (4, 8, MSF_CONTINUE), (8, 11, 0)):
+        call("msf_hist_sf_f32", plan.handle, c_p(p4[f0:f1].data_ptr()), 3000, f1 - f0, c_p(0), fl,
+             c_p(three.data_ptr()), st)
+    torch.cuda.synchronize()
+    assert torch.equal(one, three)
+    ref = ohist.hist_sf(pos.astype(np.float32), box, w, (64, 64, 64))
+    assert rel_err(one.cpu().numpy(), ref) < TOL
