@@ -59,12 +59,15 @@ def algorithmic_bytes_per_frame(n_atoms=N_ATOMS, dims=DIMS):
 
 
 class Clocks:
-    """nvidia-smi sampled during the timed region."""
+    """nvidia-smi sampled every 100 ms; only the samples stamped inside the
+    timed region (between mark_start and mark_end) are summarised.  The
+    sampler is started, and its first sample awaited, before the region."""
 
     def __init__(self, index=0):
         self.proc = None
         self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
         self.index = index
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
@@ -72,16 +75,26 @@ class Clocks:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index),
-                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "--query-gpu=timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+            deadline = time.time() + 5.0
+            while time.time() < deadline and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
 
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
     def __exit__(self, *a):
         if self.proc is not None:
+            time.sleep(0.15)   # let the sample after the region land
             self.proc.terminate()
             self.proc.wait()
             self.f.close()
@@ -89,22 +102,29 @@ class Clocks:
     def summary(self):
         if self.proc is None:
             return None
-        sm, mx, reasons = [], [], set()
+        import datetime
+        sm, mx, reasons, total = [], [], set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         try:
             for line in open(self.path):
                 f = [x.strip() for x in line.split(",")]
-                if len(f) < 9:
+                if len(f) < 10:
                     continue
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-                for n, v in zip(names, f[5:9]):
+                total += 1
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                if self.t0 is not None and not (self.t0 <= ts <= self.t1):
+                    continue
+                sm.append(float(f[2]))
+                mx.append(float(f[3]))
+                for n, v in zip(names, f[6:10]):
                     if v.lower().startswith("active"):
                         reasons.add(n)
         except Exception:
             return None
         if not sm:
-            return None
+            return {"sm_mhz": None, "sm_max_mhz": None, "samples": 0, "reasons": [],
+                    "note": f"no sample inside the timed region ({total} around it): region shorter than "
+                            "the 100 ms sampling period"}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "samples": len(sm),
                 "reasons": sorted(reasons)}
 
@@ -199,7 +219,9 @@ def run_batched_only(torch, dev, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200 for the chain: ~0.6 s, long enough for clock samples; "
+                         "5 for --impl reference; 3 for --batched-only)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=0)
@@ -215,6 +237,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = 5 if args.impl == "reference" else (3 if args.batched_only else 200)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -310,7 +334,9 @@ def main():
         return ms
 
     with Clocks(local) as clk:
+        clk.mark_start()
         ms = timed(run, args.steps)
+        clk.mark_end()
     clocks = clk.summary()
     ms_per_step = ms / args.steps
     value = FRAMES * world * args.steps / (ms / 1000.0)
