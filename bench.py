@@ -216,6 +216,44 @@ def run_batched_only(torch, dev, args):
     return 0
 
 
+def stress_512(torch, dev, steps=1, frames=40):
+    """1M atoms in a 25 nm cube (6 x 6 columns) on the 512^3 grid, `frames`
+    frames streamed from pinned host memory through mdsf.structure_factor;
+    returns (frames/s, note)."""
+    import mdsf
+    from mdsf import synth
+    from mdsf.plan import clear_plans
+    pos5, box5, w5 = synth.columnar(n_atoms=1_000_000, box=(25.0, 25.0, 25.0), n_cols=(6, 6), lattice=25.0 / 6,
+                                    frames=frames, seed=11)
+    p5 = torch.from_numpy(synth.pack_float4(pos5, w5)).pin_memory()
+    del pos5
+    mdsf.structure_factor(p5[:4], box5, None, (512, 512, 512), device=dev)     # plan + first launches
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sf5 = mdsf.structure_factor(p5, box5, None, (512, 512, 512), device=dev)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    dc = float(sf5[0, 0, 0].item())
+    assert abs(dc - frames * float(np.sum(w5, dtype=np.float64)) ** 2) < 1e-5 * dc
+    plan5 = mdsf.get_plan((512, 512, 512), box5, device=dev, max_atoms=1_000_000)
+    note = (f"1M atoms, 25 nm cube, 6x6 columns, 512^3 grid, {frames} frames streamed from pinned host memory "
+            f"(variant {plan5.tuning()['variant']}, batch {plan5.batch})")
+    del sf5, p5, plan5
+    clear_plans()
+    torch.cuda.empty_cache()
+    return frames / (ms / 1000.0), note
+
+
+def run_stress_only(torch, dev, args):
+    value, note = stress_512(torch, dev, steps=args.steps)
+    print(json.dumps({"metric": "frames/s of the 512^3 stress grid (1M atoms, streamed from host)",
+                      "value": value, "unit": "frames/s", "note": note}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -232,13 +270,15 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--stream-chunk", type=int, default=0,
                     help="frames per host->device chunk of the e2e path (0: the API default, one batch)")
+    ap.add_argument("--stress-only", action="store_true",
+                    help="only the 512^3 stress grid (1M atoms, 40 frames from pinned host memory)")
     ap.add_argument("--batched-only", action="store_true",
                     help="only the 64 uneven batched systems (one graph, 2 warm-up + `--steps` replays)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.steps is None:
-        args.steps = 5 if args.impl == "reference" else (3 if args.batched_only else 200)
+        args.steps = 5 if args.impl == "reference" else (3 if args.batched_only or args.stress_only else 200)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -257,6 +297,8 @@ def main():
     dev = torch.device("cuda", local)
     if args.batched_only:
         return run_batched_only(torch, dev, args)
+    if args.stress_only:
+        return run_stress_only(torch, dev, args)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
@@ -458,7 +500,8 @@ def main():
 
 
 def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
-    """Plain one-frame-per-launch path and the direct-sum gradient rate."""
+    """Plain one-frame-per-launch path, the direct-sum gradient rate, the
+    batched uneven systems and the 512^3 stress grid."""
     from mdsf._lib import c_p, call
     from mdsf.api import _ptr
     out = {}
@@ -532,6 +575,10 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
                                    f"{variants.count(4)} on the smooth mixed-radix chain)")
     del b, systems
     torch.cuda.empty_cache()
+
+    # large stress grid: 1M atoms in a 25 nm cube (6 x 6 columns), 512^3, frames
+    # streamed from pinned host memory through the public API (e2e)
+    out["stress_512_frames_per_s"], out["stress_512_note"] = stress_512(torch, dev)
     return out
 
 
