@@ -302,6 +302,21 @@ int msf_hist_sf_f32_noalloc(const void* pos_w, int64_t n_atoms, int64_t n_frames
                             int32_t flags, double* sf, msf_stream_t stream);
 size_t msf_noalloc_scratch_bytes(void);
 
+/* ---------------------------------------------- trajectory ingest (host)
+ * GROMACS .gro trajectories (one or more frames, fixed columns), read on the
+ * host with one thread per frame group.  Replaces the .gro reading of
+ * load_traj.py (process_gro_mdtraj, load_traj.py:91-110, through mdtraj:
+ * coordinates nm -> Angstrom x10, unitcell lengths x10; load_gro,
+ * load_traj.py:11-20: atom names from columns 11-15).
+ * msf_gro_scan: atom and frame counts (MSF_E_UNSUPPORTED when the atom count
+ * changes between frames).  msf_gro_read: xyz (n_frames, n_atoms, 3) float32
+ * Angstrom = float32(nm field) * 10 in float32; box (n_frames, 3) the box
+ * vector lengths (float32 norms) * 10; names NULL or n_atoms x 8 bytes
+ * (the first frame's atom names, NUL padded); threads 0 = all cores. */
+int msf_gro_scan(const char* path, int64_t* n_atoms, int64_t* n_frames);
+int msf_gro_read(const char* path, int64_t n_atoms, int64_t n_frames, float* xyz, double* box, char* names,
+                 int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,7 +68,7 @@ def build(force=False, verbose=False, extra=()):
             if err.strip():
                 sys.stderr.write(err)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
