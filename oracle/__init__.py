@@ -23,6 +23,8 @@ Modules (each function cites the reference file:line it follows):
   ``kgridplt``, npz layout).
 * :mod:`oracle.ewald`  -- Ewald-sphere slices of ``plot2d.py:218-267``.
 * :mod:`oracle.direct` -- FP64 direct-sum S(q) and its analytic gradient.
+* :mod:`oracle.cyl`    -- the cylindrical (r, z) average of ``plot2d.PLOT_RAD_NEW``.
+* :mod:`oracle.gro`    -- .gro trajectory ingest (``load_traj.py``).
 
 Pinning: ``tests/golden/*.npz`` hold outputs of the reference's own
 ``dens.compute_sf`` and ``plot2d.Plot_Ewald_Sphere_Correction`` run in the
