@@ -579,8 +579,43 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     # large stress grid: 1M atoms in a 25 nm cube (6 x 6 columns), 512^3, frames
     # streamed from pinned host memory through the public API (e2e)
     out["stress_512_frames_per_s"], out["stress_512_note"] = stress_512(torch, dev)
+    out.update(radial_extra(torch, dev))
     out.update(gro_ingest())
     return out
+
+
+def radial_extra(torch, dev, shape=(254, 254, 255), nbins=750, reps=5):
+    """radial_integrate (the |q|^2 float16 histogram) over the kgridplt of
+    the 256x256x128 grid: the (..., 4) array form (range pass + bin pass,
+    32 B read per voxel each) and the grid form (8 B per voxel)."""
+    from mdsf import radial as mrad
+    from mdsf.api import plot_axes
+    X, Y, Z = plot_axes((shape[0] + 2, shape[1] + 2, (shape[2] + 3) // 2), np.array([160.0, 138.56, 80.0]))
+    g = torch.Generator(device=dev).manual_seed(3)
+    S = torch.rand(shape, dtype=torch.float64, device=dev, generator=g) * 100
+    D = torch.empty(shape + (4,), dtype=torch.float64, device=dev)
+    D[..., 0] = torch.from_numpy(X).to(dev)[:, None, None]
+    D[..., 1] = torch.from_numpy(Y).to(dev)[None, :, None]
+    D[..., 2] = torch.from_numpy(Z).to(dev)[None, None, :]
+    D[..., 3] = S
+    nv = S.numel()
+    res = {}
+    for name, fn, bytes_per in (("points", lambda: mrad.radial_histograms(D, nbins), 64),
+                                ("grid", lambda: mrad.radial_histograms_grid(S, X, Y, Z, nbins), 8)):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        res[f"radial_{name}_voxels_per_s"] = nv / dt
+        res[f"radial_{name}_gbs"] = nv * bytes_per / dt / 1e9
+    res["radial_note"] = (f"{shape} voxels, {nbins} bins, float16 R and bin search as numpy; wall time per call "
+                          "incl. host range/edges and the D2H of the histograms")
+    del D, S
+    torch.cuda.empty_cache()
+    return res
 
 
 def gro_ingest(frames=8, atoms=N_ATOMS):

@@ -231,6 +231,28 @@ int msf_cyl_average(const double* D, int32_t p0, int32_t p1, int32_t p2, const d
                     const int32_t* nth, int32_t nr, const double* zar, int32_t nz, double* oa,
                     msf_stream_t stream);
 
+/* --------------------------------------------- radial integrate (|q|^2)
+ * plot2d.radial_integrate (plot2d.py:160-173): histograms of S over
+ * R = f16(qx^2) + f16(qy^2) + f16(qz^2) with numpy's float16 equal-width bin
+ * search (numpy >= 2 arithmetic: every step rounded to float16).
+ * msf_radial_range: D (n_vox, 4) FP64 (qx, qy, qz, S), 16-byte aligned;
+ *   stats (device, 3 u32) <- {min R bits, max R bits, 1 if any R is inf/NaN}.
+ * msf_radial_bin_points: D as above; edges (device) the nbins + 1 float16
+ *   edges (numpy.linspace(first, last, nbins + 1, dtype=float16), built by
+ *   the caller from the range); hist (FP64) and count (int64) accumulate
+ *   (zero them first); status bit 0 set if a bin index had to be clamped.
+ *   1 <= nbins <= 2048, else MSF_E_UNSUPPORTED.
+ * msf_radial_bin_grid: the same for the grid form of D -- S (p0, p1, p2)
+ *   FP64 with qx = X[i], qy = Y[j], qz = Z[k]; hx/hy/hz (device) the float16
+ *   tables f16(X^2), f16(Y^2), f16(Z^2).
+ */
+int msf_radial_range(const double* D, int64_t n_vox, uint32_t* stats, msf_stream_t stream);
+int msf_radial_bin_points(const double* D, int64_t n_vox, const uint16_t* edges, int32_t nbins, double* hist,
+                          int64_t* count, uint32_t* status, msf_stream_t stream);
+int msf_radial_bin_grid(const double* S, int32_t p0, int32_t p1, int32_t p2, const uint16_t* hx,
+                        const uint16_t* hy, const uint16_t* hz, const uint16_t* edges, int32_t nbins,
+                        double* hist, int64_t* count, uint32_t* status, msf_stream_t stream);
+
 /* ----------------------------------------------------- direct sum (a13)
  * S_q = |sum_j f_j exp(i q.r_j)|^2 for n_sys systems of n_atoms atoms and
  * n_q vectors each (FP32).  r_f: (n_sys, n_atoms) float4 (x, y, z, f);

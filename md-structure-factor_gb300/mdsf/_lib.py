@@ -77,6 +77,9 @@ SIGNATURES = {
     "msf_ewald": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_d, c_p, c_p, c_p, c_p]),
     "msf_cyl_average": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_int, c_p, c_int,
                                 c_p, c_p]),
+    "msf_radial_range": (c_int, [c_p, c_i64, c_p, c_p]),
+    "msf_radial_bin_points": (c_int, [c_p, c_i64, c_p, c_int, c_p, c_p, c_p, c_p]),
+    "msf_radial_bin_grid": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_int, c_p, c_p, c_p, c_p]),
     "msf_direct_fwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p]),
     "msf_direct_bwd": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_int, c_p, c_p, c_p, c_p]),
     "msf_batch_create": (c_int, [C.POINTER(c_p), C.POINTER(BatchSystem), c_int, c_int]),

@@ -2,7 +2,7 @@
 
 Run in a container where the reference checkout is present:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [--radial]
 
 It imports the reference's ``dens.py`` and ``plot2d.py`` directly (their
 missing third-party modules -- ``past.utils``, ``tqdm`` progress bars and
@@ -19,6 +19,9 @@ Fixtures:
   hist_edges.npz -- ``numpy.histogramdd`` on positions placed on and around
                   bin edges (pins the binning semantics the CUDA deposit
                   must match on numpy versions other than the one here).
+  cyl_*.npz    -- the cylindrical (r, z) average of ``PLOT_RAD_NEW``.
+  radial_*.npz -- ``plot2d.radial_integrate`` inputs and the (E[:-1], H)
+                  it plots (``--radial`` makes these alone).
 """
 from __future__ import annotations
 
@@ -207,5 +210,56 @@ def main(ref):
         print("cyl", name, np.asarray(finalT).shape)
 
 
+def radial_cases():
+    """kgridplt-shaped inputs for radial_integrate: the three compute_sf
+    fixtures (by name), a synthetic q grid reaching |q|^2 ~ 400 (float16
+    spacing 0.25 there; stored as its axes and S) and a grid of one |q|
+    (empty range, widened by 0.5)."""
+    cases = {}
+    for name in ("gauss_ortho", "gauss_tcl", "gauss_corner"):
+        D = np.load(os.path.join(HERE, name + ".npz"))["out_kgridplt"]
+        cases[name.split("_", 1)[1]] = (D, 750, dict(source=name))
+    rng = np.random.default_rng(11)
+    X = np.linspace(-12.0, 12.0, 24, endpoint=False)
+    Y = np.linspace(-10.5, 10.5, 20, endpoint=False)
+    Z = np.linspace(-9.0, 9.0, 25)
+    S = np.round(rng.gamma(2.0, 3.0, (24, 20, 25)), 3)
+    cases["wide"] = (radial_grid(X, Y, Z, S), 750, dict(X=X, Y=Y, Z=Z, S=S))
+    D1 = np.zeros((3, 4, 5, 4))
+    D1[..., 0] = 0.5
+    D1[..., 3] = np.round(rng.uniform(0, 1, (3, 4, 5)), 3)
+    cases["flat"] = (D1, 12, dict(D=D1))
+    return cases
+
+
+def radial_grid(X, Y, Z, S):
+    D = np.zeros(S.shape + (4,))
+    D[..., 0], D[..., 1], D[..., 2] = X[:, None, None], Y[None, :, None], Z[None, None, :]
+    D[..., 3] = S
+    return D
+
+
+def main_radial(ref):
+    """radial_integrate (plot2d.py:160-173) run by the reference, its
+    plt.plot(E[:-1], H) call recorded."""
+    calls = _install_stubs()
+    sys.path.insert(0, ref)
+    import plot2d
+    for name, (D, nb, store) in radial_cases().items():
+        del calls[:]
+        with contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
+            plot2d.radial_integrate(D.copy(), nb, "radial.png")
+        pl = [c for c in calls if c[0] == "plot"][0]
+        np.savez_compressed(os.path.join(HERE, "radial_" + name + ".npz"), nbins=nb,
+                            E=np.asarray(pl[1][0]), H=np.asarray(pl[1][1]), **store)
+        print("radial", name, D.shape, nb)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_dir = args[0] if args else "/root/reference"
+    if "--radial" in sys.argv:
+        main_radial(ref_dir)
+    else:
+        main(ref_dir)
+        main_radial(ref_dir)
