@@ -580,6 +580,7 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     # streamed from pinned host memory through the public API (e2e)
     out["stress_512_frames_per_s"], out["stress_512_note"] = stress_512(torch, dev)
     out.update(radial_extra(torch, dev))
+    out.update(rz_extra(torch, dev))
     out.update(gro_ingest())
     return out
 
@@ -616,6 +617,30 @@ def radial_extra(torch, dev, shape=(254, 254, 255), nbins=750, reps=5):
     del D, S
     torch.cuda.empty_cache()
     return res
+
+
+def rz_extra(torch, dev, shape=(254, 254, 255), reps=3):
+    """(r, z) histograms of measure_intensity.py over the kgridplt of the
+    256x256x128 grid in the 120-degree cell: shear, trilinear interpolation,
+    r/z bin search and FP64 atomics per voxel."""
+    from mdsf import rz as mrz
+    from mdsf.api import plot_axes
+    X, Y, Z = plot_axes((shape[0] + 2, shape[1] + 2, (shape[2] + 3) // 2), np.array([160.0, 138.56, 80.0]))
+    g = torch.Generator(device=dev).manual_seed(4)
+    S = torch.rand(shape, dtype=torch.float64, device=dev, generator=g) * 100
+    th = 120 * np.pi / 180.0
+    ucell = np.array([[1, 0, 0], [np.cos(th), np.sin(th), 0], [0, 0, 1]])
+    mrz.rz_histogram(S, X, Y, Z, ucell)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        mrz.rz_histogram(S, X, Y, Z, ucell)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    del S
+    return {"rz_voxels_per_s": shape[0] * shape[1] * shape[2] / dt,
+            "rz_note": f"{shape} voxels, r/z edges = the x/z axes, theta = 120 deg cell, linear weights; wall time "
+                       "per call incl. the D2H of the two histograms"}
 
 
 def gro_ingest(frames=8, atoms=N_ATOMS):

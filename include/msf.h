@@ -231,6 +231,22 @@ int msf_cyl_average(const double* D, int32_t p0, int32_t p1, int32_t p2, const d
                     const int32_t* nth, int32_t nr, const double* zar, int32_t nz, double* oa,
                     msf_stream_t stream);
 
+/* ------------------------------------------------ (r, z) histograms
+ * measure_intensity.py:58-120 (and plot2d.py:1035-1147): each voxel of the
+ * centred S (p0, p1, p2) with axes X, Y, Z moves to
+ * p = X[ix] b1 + Y[iy] b2 + Z[iz] b3 (b_host: rows b1, b2, b3, 9 doubles,
+ * host memory); weight = S interpolated at p (mode 0: trilinear on the
+ * original axes, NaN outside) or the voxel's own S (mode 1); r =
+ * sqrt(px^2 + py^2) and pz are binned with numpy.histogram2d's explicit
+ * edges (ascending; the last edge closes the last bin; outside or NaN
+ * dropped) into hval (FP64 sums) and hcount (int64), both
+ * (n_r_edges - 1) x (n_z_edges - 1) row major; they accumulate (zero them
+ * first).
+ */
+int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X, const double* Y,
+                const double* Z, const double* b_host, int32_t mode, const double* r_edges, int32_t n_r_edges,
+                const double* z_edges, int32_t n_z_edges, double* hval, int64_t* hcount, msf_stream_t stream);
+
 /* --------------------------------------------- radial integrate (|q|^2)
  * plot2d.radial_integrate (plot2d.py:160-173): histograms of S over
  * R = f16(qx^2) + f16(qy^2) + f16(qz^2) with numpy's float16 equal-width bin

@@ -151,9 +151,92 @@ __global__ void k_cyl(CylArgs a) {
   }
 }
 
+// The (r, z) histograms of measure_intensity.py:58-120 (and the same steps
+// in plot2d.py:1035-1147): every voxel (ix, iy, iz) of the centred grid is
+// moved to p = X[ix] b1 + Y[iy] b2 + Z[iz] b3, accumulated per component in
+// numpy's order ((X b1 + Y b2) + Z b3); its weight is S interpolated at p on
+// the original axes (RegularGridInterpolator, linear, NaN outside; mode 0)
+// or the voxel's own S (mode 1: the nearest-neighbour interpolator of the
+// sheared grid evaluated at its own nodes, plot2d.py:1093-1101); r =
+// sqrt(px^2 + py^2), z = pz; both binned with numpy.histogramdd's explicit
+// edges (searchsorted right, a value equal to the last edge in the last bin,
+// anything else outside -- or NaN -- dropped).  FP64 sums and int64 counts
+// by global atomics.
+struct RzArgs {
+  const double* S;
+  int p0, p1, p2;
+  const double* X;
+  const double* Y;
+  const double* Z;
+  double b[9];          // rows b1, b2, b3
+  int mode;
+  const double* re;     // r edges (nre)
+  int nre;
+  const double* ze;     // z edges (nze)
+  int nze;
+  double* hval;         // (nre - 1) x (nze - 1)
+  unsigned long long* hcount;
+};
+
+// histogramdd's bin of v for ascending edges e[0..n-1]: -1 when dropped
+__device__ __forceinline__ int edge_bin(const double* __restrict__ e, int n, double v) {
+  int lo = 0, hi = n;   // count of edges <= v (searchsorted right)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(e + mid) <= v) lo = mid + 1; else hi = mid;
+  }
+  if (v == __ldg(e + n - 1)) lo = n - 1;
+  return (lo >= 1 && lo <= n - 1) ? lo - 1 : -1;
+}
+
+__global__ void k_rz_hist(RzArgs a) {
+  const int64_t total = (int64_t)a.p0 * a.p1 * a.p2;
+  const int nz = a.nze - 1;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(e % a.p2);
+    const int64_t t = e / a.p2;
+    const int iy = (int)(t % a.p1), ix = (int)(t / a.p1);
+    const double xv = __ldg(a.X + ix), yv = __ldg(a.Y + iy), zv = __ldg(a.Z + iz);
+    double p[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      p[c] = __dadd_rn(__dadd_rn(__dmul_rn(xv, a.b[c]), __dmul_rn(yv, a.b[3 + c])), __dmul_rn(zv, a.b[6 + c]));
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])));
+    const int br = edge_bin(a.re, a.nre, r);
+    const int bz = edge_bin(a.ze, a.nze, p[2]);
+    if (br < 0 || bz < 0) continue;
+    const double w = a.mode == 0 ? interp3(a.S, a.p0, a.p1, a.p2, a.X, a.Y, a.Z, p[0], p[1], p[2]) : __ldg(a.S + e);
+    const int64_t bin = (int64_t)br * nz + bz;
+    atomicAdd(a.hval + bin, w);
+    atomicAdd(a.hcount + bin, 1ull);
+  }
+}
+
 }  // namespace msf
 
 using namespace msf;
+
+extern "C" int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X, const double* Y,
+                           const double* Z, const double* b_host, int32_t mode, const double* r_edges,
+                           int32_t n_r_edges, const double* z_edges, int32_t n_z_edges, double* hval,
+                           int64_t* hcount, msf_stream_t stream) {
+  if (!S || !X || !Y || !Z || !b_host || !r_edges || !z_edges || !hval || !hcount) return MSF_E_INVALID;
+  if (p0 < 2 || p1 < 2 || p2 < 2 || n_r_edges < 2 || n_z_edges < 2 || (mode != 0 && mode != 1))
+    return MSF_E_INVALID;
+  RzArgs a;
+  a.S = S; a.p0 = p0; a.p1 = p1; a.p2 = p2;
+  a.X = X; a.Y = Y; a.Z = Z;
+  for (int i = 0; i < 9; ++i) a.b[i] = b_host[i];
+  a.mode = mode;
+  a.re = r_edges; a.nre = n_r_edges; a.ze = z_edges; a.nze = n_z_edges;
+  a.hval = hval;
+  a.hcount = reinterpret_cast<unsigned long long*>(hcount);
+  const int64_t total = (int64_t)p0 * p1 * p2;
+  const int blocks = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
+  k_rz_hist<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
+  return launch_status();
+}
 
 extern "C" int msf_cyl_average(const double* D, int32_t p0, int32_t p1, int32_t p2, const double* X,
                                const double* Y, const double* Z, const double* b_inv_host,

@@ -77,6 +77,8 @@ SIGNATURES = {
     "msf_ewald": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_d, c_p, c_p, c_p, c_p]),
     "msf_cyl_average": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_int, c_p, c_int,
                                 c_p, c_p]),
+    "msf_rz_hist": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_int, c_p, c_int, c_p, c_int, c_p, c_p,
+                            c_p]),
     "msf_radial_range": (c_int, [c_p, c_i64, c_p, c_p]),
     "msf_radial_bin_points": (c_int, [c_p, c_i64, c_p, c_int, c_p, c_p, c_p, c_p]),
     "msf_radial_bin_grid": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_int, c_p, c_p, c_p, c_p]),

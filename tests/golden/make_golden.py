@@ -2,7 +2,7 @@
 
 Run in a container where the reference checkout is present:
 
-    python tests/golden/make_golden.py /root/reference [--radial]
+    python tests/golden/make_golden.py /root/reference [--radial | --rz]
 
 It imports the reference's ``dens.py`` and ``plot2d.py`` directly (their
 missing third-party modules -- ``past.utils``, ``tqdm`` progress bars and
@@ -22,6 +22,9 @@ Fixtures:
   cyl_*.npz    -- the cylindrical (r, z) average of ``PLOT_RAD_NEW``.
   radial_*.npz -- ``plot2d.radial_integrate`` inputs and the (E[:-1], H)
                   it plots (``--radial`` makes these alone).
+  rz_*.npz     -- ``measure_intensity.py`` run as a script: the inputs and
+                  outputs of its two ``histogram2d`` calls, the plotted Hrz
+                  and the line it writes (``--rz`` makes these alone).
 """
 from __future__ import annotations
 
@@ -255,11 +258,68 @@ def main_radial(ref):
         print("radial", name, D.shape, nb)
 
 
+def main_rz(ref):
+    """measure_intensity.py run as a script (``-l <kgridplt npz> -f -y``) on
+    the compute_sf fixtures.  numpy >= 1.24 no longer takes its
+    ``histogram2d(..., normed=)``; a wrapper passes it on as ``density=`` (the
+    same histogramdd option) and records the inputs and outputs of both
+    calls.  PIL and the interactive plotting are stubbed."""
+    import runpy
+    calls = _install_stubs()
+    import matplotlib.pyplot as plt
+    plt.pcolormesh = lambda *a, **k: calls.append(("pcolormesh", a, k))
+    plt.show = lambda *a, **k: None
+    pil = types.ModuleType("PIL")
+    pil.Image = types.ModuleType("PIL.Image")
+    tq = types.ModuleType("tqdm")
+    tq.trange = range
+    tq.tqdm = _Quiet
+    sys.modules.update({"PIL": pil, "PIL.Image": pil.Image, "tqdm": tq})
+    rec = []
+    real = np.histogram2d
+
+    def histogram2d(x, y, bins=10, range=None, normed=None, weights=None, density=None):
+        out = real(x, y, bins=bins, range=range, weights=weights, density=normed if normed is not None else density)
+        rec.append(dict(x=np.array(x), y=np.array(y), w=None if weights is None else np.array(weights),
+                        H=out[0], density=bool(normed or density)))
+        return out
+    cwd = os.getcwd()
+    tmp = os.path.join(tempfile.gettempdir(), "mdsfgolden")
+    os.makedirs(tmp, exist_ok=True)
+    np.histogram2d = histogram2d
+    try:
+        for name in ("gauss_ortho", "gauss_tcl"):
+            D = np.load(os.path.join(HERE, name + ".npz"))["out_kgridplt"]
+            os.chdir(tmp)
+            np.savez("out_x_sf_7.npz", kgridplt=D)
+            if os.path.exists("intens.txt"):
+                os.remove("intens.txt")
+            del calls[:], rec[:]
+            sys.argv = ["measure_intensity.py", "-l", "out_x_sf_7.npz", "-f", "-y", "-o", "intens.txt"]
+            with contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
+                runpy.run_path(os.path.join(ref, "measure_intensity.py"), run_name="__main__")
+            line = open("intens.txt").read()
+            os.chdir(cwd)
+            pc = [c for c in calls if c[0] == "pcolormesh"][0]
+            cnt = [r for r in rec if r["w"] is None][0]
+            val = [r for r in rec if r["w"] is not None][0]
+            np.savez_compressed(os.path.join(HERE, "rz_" + name.split("_", 1)[1] + ".npz"), source=name,
+                                rpts=val["x"], zpts=val["y"], w=val["w"], Hcount=cnt["H"], Hval_density=val["H"],
+                                HrzT=np.asarray(pc[1][2]), line=line)
+            print("rz", name, val["H"].shape, np.isnan(val["w"]).sum(), repr(line))
+    finally:
+        np.histogram2d = real
+        os.chdir(cwd)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_dir = args[0] if args else "/root/reference"
     if "--radial" in sys.argv:
         main_radial(ref_dir)
+    elif "--rz" in sys.argv:
+        main_rz(ref_dir)
     else:
         main(ref_dir)
         main_radial(ref_dir)
+        main_rz(ref_dir)
