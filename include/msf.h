@@ -247,6 +247,20 @@ int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, const doubl
                 const double* Z, const double* b_host, int32_t mode, const double* r_edges, int32_t n_r_edges,
                 const double* z_edges, int32_t n_z_edges, double* hval, int64_t* hcount, msf_stream_t stream);
 
+/* ------------------------------------- nearest node of a sheared grid
+ * NearestNDInterpolator over the transformed grid of plot2d.py:1087-1101
+ * (the non-orthorhombic branch; a KD-tree there): out[e] = S at the node
+ * p(i,j,k) = X[i] b1 + Y[j] b2 + Z[k] b3 nearest q[e] (FP64 squared
+ * Euclidean distance; ties to the lowest flat index; NaN for a NaN query).
+ * lattice_host (24 doubles, host): b1 b2 b3 (rows), p(0,0,0), the inverse of
+ * M = rows (dX b1, dY b2, dZ b3) with the mean axis steps, and the norms of
+ * that inverse's columns.  index (optional, device, m int64) receives the
+ * node's flat index.
+ */
+int msf_nearest_sheared(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X, const double* Y,
+                        const double* Z, const double* lattice_host, const double* q, int64_t m, double* out,
+                        int64_t* index, msf_stream_t stream);
+
 /* --------------------------------------------- radial integrate (|q|^2)
  * plot2d.radial_integrate (plot2d.py:160-173): histograms of S over
  * R = f16(qx^2) + f16(qy^2) + f16(qz^2) with numpy's float16 equal-width bin

@@ -213,9 +213,114 @@ __global__ void k_rz_hist(RzArgs a) {
   }
 }
 
+// NearestNDInterpolator over the sheared grid (plot2d.py:1087-1101): the
+// nodes are p(i, j, k) = X[i] b1 + Y[j] b2 + Z[k] b3 (numpy's order per
+// component, as k_rz_hist), the value at a query q is S at the node nearest
+// q in FP64 squared Euclidean distance ((dx^2 + dy^2) + dz^2, scipy's
+// cKDTree order).  Search: f = (q - o) Minv, the query's fractional index
+// in the lattice o + (i, j, k) M (M rows dX b1, dY b2, dZ b3, uniform-axis
+// steps); the node round(f) clamped to the grid is at distance rho, and
+// every node within rho of q has |i_a - f_a| <= rho * |Minv column a|, so
+// the box f_a -+ (rho |Minv_a| + 1) clamped to the grid holds the nearest
+// node (the +1 absorbs the axes' rounding).  Ties go to the lowest flat
+// index (C order).
+struct NearestArgs {
+  const double* S;
+  int p0, p1, p2;
+  const double* X;
+  const double* Y;
+  const double* Z;
+  double b[9];      // rows b1, b2, b3
+  double o[3];      // p(0, 0, 0)
+  double minv[9];   // inverse of M (row major)
+  double cn[3];     // Euclidean norms of the columns of minv
+  const double* q;  // (m, 3)
+  int64_t m;
+  double* out;
+  int64_t* index;   // optional: flat index of the nearest node
+};
+
+__device__ __forceinline__ void node_pos(const NearestArgs& a, int i, int j, int k, double* p) {
+  const double xv = __ldg(a.X + i), yv = __ldg(a.Y + j), zv = __ldg(a.Z + k);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    p[c] = __dadd_rn(__dadd_rn(__dmul_rn(xv, a.b[c]), __dmul_rn(yv, a.b[3 + c])), __dmul_rn(zv, a.b[6 + c]));
+}
+
+__device__ __forceinline__ double dist2(const double* p, double qx, double qy, double qz) {
+  const double dx = __dsub_rn(p[0], qx), dy = __dsub_rn(p[1], qy), dz = __dsub_rn(p[2], qz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__global__ void k_nearest(NearestArgs a) {
+  const int n[3] = {a.p0, a.p1, a.p2};
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.m; e += (int64_t)gridDim.x * blockDim.x) {
+    const double qx = __ldg(a.q + 3 * e), qy = __ldg(a.q + 3 * e + 1), qz = __ldg(a.q + 3 * e + 2);
+    const double d[3] = {qx - a.o[0], qy - a.o[1], qz - a.o[2]};
+    double f[3];
+    int c0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      f[c] = d[0] * a.minv[c] + d[1] * a.minv[3 + c] + d[2] * a.minv[6 + c];
+      const double r = rint(f[c]);
+      c0[c] = r < 0.0 ? 0 : (r > (double)(n[c] - 1) ? n[c] - 1 : (int)r);
+    }
+    double p[3];
+    node_pos(a, c0[0], c0[1], c0[2], p);
+    double best = dist2(p, qx, qy, qz);
+    if (!(best == best)) {   // NaN query: scipy's tree gives no finite neighbour
+      a.out[e] = __longlong_as_double(0x7ff8000000000000LL);
+      if (a.index) a.index[e] = -1;
+      continue;
+    }
+    int64_t bi = ((int64_t)c0[0] * a.p1 + c0[1]) * a.p2 + c0[2];
+    const double rho = sqrt(best);
+    int lo[3], hi[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double w = rho * a.cn[c] + 1.0;
+      const double l = floor(f[c] - w), h = ceil(f[c] + w);
+      lo[c] = l < 0.0 ? 0 : (l > (double)(n[c] - 1) ? n[c] - 1 : (int)l);
+      hi[c] = h < 0.0 ? 0 : (h > (double)(n[c] - 1) ? n[c] - 1 : (int)h);
+    }
+    for (int i = lo[0]; i <= hi[0]; ++i)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int k = lo[2]; k <= hi[2]; ++k) {
+          node_pos(a, i, j, k, p);
+          const double d2 = dist2(p, qx, qy, qz);
+          const int64_t fi = ((int64_t)i * a.p1 + j) * a.p2 + k;
+          if (d2 < best || (d2 == best && fi < bi)) { best = d2; bi = fi; }
+        }
+    a.out[e] = __ldg(a.S + bi);
+    if (a.index) a.index[e] = bi;
+  }
+}
+
 }  // namespace msf
 
 using namespace msf;
+
+extern "C" int msf_nearest_sheared(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X,
+                                   const double* Y, const double* Z, const double* lattice_host,
+                                   const double* q, int64_t m, double* out, int64_t* index, msf_stream_t stream) {
+  if (!S || !X || !Y || !Z || !lattice_host || (!q && m) || (!out && m) || m < 0) return MSF_E_INVALID;
+  if (p0 < 1 || p1 < 1 || p2 < 1) return MSF_E_INVALID;
+  if (m == 0) return MSF_OK;
+  NearestArgs a;
+  a.S = S; a.p0 = p0; a.p1 = p1; a.p2 = p2;
+  a.X = X; a.Y = Y; a.Z = Z;
+  for (int i = 0; i < 9; ++i) a.b[i] = lattice_host[i];
+  for (int i = 0; i < 3; ++i) a.o[i] = lattice_host[9 + i];
+  for (int i = 0; i < 9; ++i) a.minv[i] = lattice_host[12 + i];
+  for (int i = 0; i < 3; ++i) {
+    a.cn[i] = lattice_host[21 + i];
+    if (!(a.cn[i] >= 0.0) || a.cn[i] > 1e300) return MSF_E_INVALID;
+  }
+  a.q = q; a.m = m; a.out = out; a.index = index;
+  const int blocks = (int)((m + 127) / 128 < 152 * 16 ? (m + 127) / 128 : 152 * 16);
+  k_nearest<<<blocks, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
+  return launch_status();
+}
 
 extern "C" int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X, const double* Y,
                            const double* Z, const double* b_host, int32_t mode, const double* r_edges,

@@ -79,6 +79,7 @@ SIGNATURES = {
                                 c_p, c_p]),
     "msf_rz_hist": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_int, c_p, c_int, c_p, c_int, c_p, c_p,
                             c_p]),
+    "msf_nearest_sheared": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_p, c_i64, c_p, c_p, c_p]),
     "msf_radial_range": (c_int, [c_p, c_i64, c_p, c_p]),
     "msf_radial_bin_points": (c_int, [c_p, c_i64, c_p, c_int, c_p, c_p, c_p, c_p]),
     "msf_radial_bin_grid": (c_int, [c_p, c_int, c_int, c_int, c_p, c_p, c_p, c_p, c_int, c_p, c_p, c_p, c_p]),

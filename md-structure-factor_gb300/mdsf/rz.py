@@ -127,3 +127,39 @@ def measure_intensity(kgridplt, box=(63, 73, 60, 40), full=False, device=None):
     crop = Hrz.T[by:ty, lx:rx]
     with np.errstate(invalid="ignore"):
         return np.mean(crop), np.amax(crop), Hrz
+
+
+def lattice_params(X, Y, Z, ucell):
+    """The 24 doubles msf_nearest_sheared takes: reciprocal rows, the first
+    node, the inverse of the step lattice and its column norms."""
+    X, Y, Z = (np.asarray(a, np.float64) for a in (X, Y, Z))
+    b = reciprocal_rows(ucell)
+    o = (X[0] * b[0] + Y[0] * b[1]) + Z[0] * b[2]
+    steps = [(a[-1] - a[0]) / (len(a) - 1) if len(a) > 1 else 1.0 for a in (X, Y, Z)]
+    M = np.vstack([steps[i] * b[i] for i in range(3)])
+    minv = np.linalg.inv(M)
+    cn = np.sqrt((minv ** 2).sum(axis=0))
+    return np.ascontiguousarray(np.concatenate([b.ravel(), o, minv.ravel(), cn]))
+
+
+def nearest_sheared(S, X, Y, Z, ucell, points, return_index=False):
+    """NearestNDInterpolator(transformed nodes, S.ravel())(points) of
+    plot2d.py:1087-1101 on the GPU: S (p0, p1, p2) CUDA float64 with axes
+    X, Y, Z, nodes moved to the reciprocal basis of ``ucell``; points (m, 3)
+    numpy or CUDA float64.  Returns a CUDA float64 (m,) tensor (and the
+    nodes' flat indices)."""
+    dev = S.device
+    S = S.to(torch.float64).contiguous()
+    p0, p1, p2 = S.shape
+    if (len(X), len(Y), len(Z)) != (p0, p1, p2):
+        raise ValueError("axes must match the grid shape")
+    lat = lattice_params(X, Y, Z, ucell)
+    with torch.cuda.device(dev):
+        q = to_device(points, dev, torch.float64).reshape(-1, 3).contiguous()
+        m = q.shape[0]
+        out = torch.empty(m, dtype=torch.float64, device=dev)
+        idx = torch.empty(m, dtype=torch.int64, device=dev) if return_index else None
+        Xd, Yd, Zd = (to_device(np.ascontiguousarray(np.asarray(a, np.float64)), dev) for a in (X, Y, Z))
+        call("msf_nearest_sheared", _ptr(S), p0, p1, p2, _ptr(Xd), _ptr(Yd), _ptr(Zd), c_p(lat.ctypes.data),
+             _ptr(q), m, _ptr(out), _ptr(idx) if idx is not None else c_p(0), stream_ptr(dev))
+    return (out, idx) if return_index else out

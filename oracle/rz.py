@@ -67,3 +67,16 @@ def rz_average(Hval, Hcount):
     for ir in range(Hrz.shape[0] // 2):
         Hrz[-ir + Hrz.shape[0] // 2, :] = Hrz[ir + 1 + Hrz.shape[0] // 2, :]
     return Hrz
+
+
+def nearest_sheared(D, ucell, points):
+    """plot2d.py:1087-1101: NearestNDInterpolator over the transformed nodes
+    (the non-orthorhombic branch), evaluated at ``points``; also the nodes'
+    flat indices from the same KD-tree query."""
+    from scipy.interpolate import NearestNDInterpolator
+    pts, _ = transformed_points(D.copy(), ucell)
+    coords = list(zip(pts[:, 0], pts[:, 1], pts[:, 2]))
+    ES = NearestNDInterpolator(coords, D[:, :, :, 3].ravel())
+    vals = ES(points)
+    _, idx = ES.tree.query(points)
+    return vals, idx
