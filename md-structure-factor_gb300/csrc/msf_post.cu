@@ -48,8 +48,9 @@ __device__ __forceinline__ int find_interval(const double* __restrict__ x, int n
   if (!(a <= v && v <= b)) return -1;
   if (v == b) return n - 2;
   const double h = __ddiv_rn(__dsub_rn(b, a), (double)(n - 1));
-  int i = (int)((v - a) / h);
-  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  // first guess, clamped before the conversion (NaN -> 0), then corrected
+  const double g = (v - a) / h;
+  int i = g >= (double)(n - 2) ? n - 2 : (g >= 0.0 ? (int)g : 0);
   while (i > 0 && v < __ldg(x + i)) --i;
   while (i < n - 2 && v >= __ldg(x + i + 1)) ++i;
   return i;
@@ -223,7 +224,8 @@ __global__ void k_rz_hist(RzArgs a) {
 // every node within rho of q has |i_a - f_a| <= rho * |Minv column a|, so
 // the box f_a -+ (rho |Minv_a| + 1) clamped to the grid holds the nearest
 // node (the +1 absorbs the axes' rounding).  Ties go to the lowest flat
-// index (C order).
+// index (C order).  A query with a NaN or infinite coordinate gets NaN
+// (index -1) before any index arithmetic.
 struct NearestArgs {
   const double* S;
   int p0, p1, p2;
@@ -252,36 +254,42 @@ __device__ __forceinline__ double dist2(const double* p, double qx, double qy, d
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// an index from a real number, clamped to [0, n-1]; NaN gives 0 (never
+// converted: a NaN to int conversion is undefined)
+__device__ __forceinline__ int clamp_index(double r, int n) {
+  if (!(r >= 0.0)) return 0;
+  if (r >= (double)(n - 1)) return n - 1;
+  return (int)r;
+}
+
 __global__ void k_nearest(NearestArgs a) {
   const int n[3] = {a.p0, a.p1, a.p2};
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.m; e += (int64_t)gridDim.x * blockDim.x) {
     const double qx = __ldg(a.q + 3 * e), qy = __ldg(a.q + 3 * e + 1), qz = __ldg(a.q + 3 * e + 2);
+    if (!(isfinite(qx) && isfinite(qy) && isfinite(qz))) {   // no finite nearest node: NaN
+      a.out[e] = __longlong_as_double(0x7ff8000000000000LL);
+      if (a.index) a.index[e] = -1;
+      continue;
+    }
     const double d[3] = {qx - a.o[0], qy - a.o[1], qz - a.o[2]};
     double f[3];
     int c0[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       f[c] = d[0] * a.minv[c] + d[1] * a.minv[3 + c] + d[2] * a.minv[6 + c];
-      const double r = rint(f[c]);
-      c0[c] = r < 0.0 ? 0 : (r > (double)(n[c] - 1) ? n[c] - 1 : (int)r);
+      c0[c] = clamp_index(rint(f[c]), n[c]);
     }
     double p[3];
     node_pos(a, c0[0], c0[1], c0[2], p);
     double best = dist2(p, qx, qy, qz);
-    if (!(best == best)) {   // NaN query: scipy's tree gives no finite neighbour
-      a.out[e] = __longlong_as_double(0x7ff8000000000000LL);
-      if (a.index) a.index[e] = -1;
-      continue;
-    }
     int64_t bi = ((int64_t)c0[0] * a.p1 + c0[1]) * a.p2 + c0[2];
     const double rho = sqrt(best);
     int lo[3], hi[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const double w = rho * a.cn[c] + 1.0;
-      const double l = floor(f[c] - w), h = ceil(f[c] + w);
-      lo[c] = l < 0.0 ? 0 : (l > (double)(n[c] - 1) ? n[c] - 1 : (int)l);
-      hi[c] = h < 0.0 ? 0 : (h > (double)(n[c] - 1) ? n[c] - 1 : (int)h);
+      lo[c] = clamp_index(floor(f[c] - w), n[c]);
+      hi[c] = clamp_index(ceil(f[c] + w), n[c]);
     }
     for (int i = lo[0]; i <= hi[0]; ++i)
       for (int j = lo[1]; j <= hi[1]; ++j)

@@ -88,7 +88,9 @@ struct BinCtx {
     unsigned short t = f2h(__fsub_rn(fr, first));
     t = f2h(__fdiv_rn(h2f(t), den));
     t = f2h(__fmul_rn(h2f(t), fn));
-    int i = (int)h2f(t);
+    const float ft = h2f(t);   // in [0, n] for R in [first, last]; clamped before the conversion
+    if (!(ft >= 0.f && ft <= (float)n)) bad = 1u;
+    int i = ft >= (float)n ? n : (ft >= 0.f ? (int)ft : 0);
     if (i == n) --i;
     if (i < 0 || i > n - 1) { bad = 1u; i = i < 0 ? 0 : n - 1; }
     if (fr < h2f(es[i])) --i;

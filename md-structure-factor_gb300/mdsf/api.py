@@ -60,6 +60,17 @@ def _ptr(t):
 _side_streams = {}
 
 
+def check_axes(*axes):
+    """RegularGridInterpolator's condition on grid axes: 1-D, finite,
+    strictly ascending (the GPU interpolation assumes it)."""
+    for i, a in enumerate(axes):
+        a = np.asarray(a, np.float64)
+        if a.ndim != 1 or a.size < 2 or not np.all(np.isfinite(a)):
+            raise ValueError(f"axis {i} must be a finite 1-D array of at least 2 points")
+        if not np.all(np.diff(a) > 0):
+            raise ValueError(f"The points in dimension {i} must be strictly ascending")
+
+
 def _side_stream(device):
     s = _side_streams.get(device)
     if s is None:
@@ -231,10 +242,14 @@ def plot_axes(half_shape, L):
 def ewald_slices(D, X, Y, Z, wavelength):
     """Ewald-sphere slices (xy, xz, yz) of D (p0, p1, p2) with axes X, Y, Z."""
     dev = D.device
-    X = to_device(np.asarray(X, np.float64), dev)
-    Y = to_device(np.asarray(Y, np.float64), dev)
-    Z = to_device(np.asarray(Z, np.float64), dev)
     p0, p1, p2 = D.shape
+    if not any(isinstance(a, torch.Tensor) for a in (X, Y, Z)):
+        check_axes(X, Y, Z)
+    if (len(X), len(Y), len(Z)) != (p0, p1, p2):
+        raise ValueError("axes must match the grid shape")
+    X = to_device(np.asarray(X, np.float64) if not isinstance(X, torch.Tensor) else X, dev, torch.float64)
+    Y = to_device(np.asarray(Y, np.float64) if not isinstance(Y, torch.Tensor) else Y, dev, torch.float64)
+    Z = to_device(np.asarray(Z, np.float64) if not isinstance(Z, torch.Tensor) else Z, dev, torch.float64)
     xy = torch.empty((p0, p1), dtype=torch.float64, device=dev)
     xz = torch.empty((p0, p2), dtype=torch.float64, device=dev)
     yz = torch.empty((p1, p2), dtype=torch.float64, device=dev)
@@ -264,6 +279,9 @@ def cylindrical_average(D, X, Y, Z, ucell, format=False):
     X = np.asarray(X, np.float64)
     Y = np.asarray(Y, np.float64)
     Z = np.asarray(Z, np.float64)
+    check_axes(X, Y, Z)
+    if (len(X), len(Y), len(Z)) != tuple(D.shape):
+        raise ValueError("axes must match the grid shape")
     u = np.asarray(ucell, np.float64)
     a1, a2, a3 = u[0], u[1], u[2]
     b1 = (np.cross(a2, a3)) / (np.dot(a1, np.cross(a2, a3)))

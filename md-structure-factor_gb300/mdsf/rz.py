@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from ._lib import c_p, call
-from .api import _ptr, to_device
+from .api import _ptr, check_axes, to_device
 from .plan import stream_ptr
 
 WEIGHTS = {"linear": 0, "self": 1}
@@ -55,6 +55,8 @@ def rz_histogram(S, X, Y, Z, ucell, r_edges=None, z_edges=None, weights="linear"
     X = np.ascontiguousarray(np.asarray(X, np.float64))
     Y = np.ascontiguousarray(np.asarray(Y, np.float64))
     Z = np.ascontiguousarray(np.asarray(Z, np.float64))
+    if weights == "linear":
+        check_axes(X, Y, Z)
     re = _edges(X if r_edges is None else r_edges, "r")
     ze = _edges(Z if z_edges is None else z_edges, "z")
     dev = S.device
@@ -154,6 +156,8 @@ def nearest_sheared(S, X, Y, Z, ucell, points, return_index=False):
     if (len(X), len(Y), len(Z)) != (p0, p1, p2):
         raise ValueError("axes must match the grid shape")
     lat = lattice_params(X, Y, Z, ucell)
+    if not np.all(np.isfinite(lat)):
+        raise ValueError("the sheared lattice is singular or not finite")
     with torch.cuda.device(dev):
         q = to_device(points, dev, torch.float64).reshape(-1, 3).contiguous()
         m = q.shape[0]

@@ -48,5 +48,17 @@ def test_nearest_at_own_nodes_is_identity_and_nan_query():
     nodes, _ = orz.transformed_points(D, cell(120.0))
     got = mrz.nearest_sheared(torch.from_numpy(S).cuda(), X, Y, Z, cell(120.0), nodes).cpu().numpy()
     np.testing.assert_array_equal(got, S.ravel())
-    nanq = np.array([[np.nan, 0.0, 0.0]])
-    assert np.isnan(mrz.nearest_sheared(torch.from_numpy(S).cuda(), X, Y, Z, cell(120.0), nanq).cpu().numpy()[0])
+    bad = np.array([[np.nan, 0.0, 0.0], [0.0, np.inf, 0.0], [0.0, 0.0, -np.inf], [0.1, 0.2, 0.3]])
+    got, idx = mrz.nearest_sheared(torch.from_numpy(S).cuda(), X, Y, Z, cell(120.0), bad, return_index=True)
+    got, idx = got.cpu().numpy(), idx.cpu().numpy()
+    assert np.all(np.isnan(got[:3])) and np.all(idx[:3] == -1)
+    want, widx = orz.nearest_sheared(D, cell(120.0), bad[3:])
+    assert got[3] == want[0] and idx[3] == widx[0]
+
+
+def test_singular_cell_raises():
+    X, Y, Z = plot_axes((8, 8, 5), np.array([4.0, 4.0, 4.0]))
+    S = torch.zeros((6, 6, 7), dtype=torch.float64, device="cuda")
+    flat = np.array([[1, 0, 0], [1, 0, 0], [0, 0, 1.0]])
+    with pytest.raises(Exception):
+        mrz.nearest_sheared(S, X, Y, Z, flat, np.zeros((1, 3)))

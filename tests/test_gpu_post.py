@@ -68,3 +68,14 @@ def test_cylindrical_average_vs_reference(name):
     np.testing.assert_array_equal(rfin, z["rfin"])
     np.testing.assert_array_equal(zfin, z["zfin"])
     np.testing.assert_allclose(final, z["final"], rtol=1e-11, atol=0)
+
+
+def test_axes_checked_before_the_gpu():
+    S = torch.zeros((5, 6, 7), dtype=torch.float64, device="cuda")
+    X, Y, Z = np.linspace(-1, 1, 5), np.linspace(-1, 1, 6), np.linspace(-1, 1, 7)
+    with pytest.raises(ValueError):
+        mdsf.ewald_slices(S, X[:4], Y, Z, 1.5)          # shorter than the grid
+    with pytest.raises(ValueError):
+        mdsf.ewald_slices(S, X[::-1], Y, Z, 1.5)        # descending
+    with pytest.raises(ValueError):
+        mdsf.cylindrical_average(S, X, np.zeros(6), Z, np.eye(3))
