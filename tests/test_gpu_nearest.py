@@ -45,6 +45,7 @@ def test_nearest_at_own_nodes_is_identity_and_nan_query():
     S = np.arange(np.prod(shape), dtype=np.float64).reshape(shape)
     D = np.zeros(shape + (4,))
     D[..., 0], D[..., 1], D[..., 2] = X[:, None, None], Y[None, :, None], Z[None, None, :]
+    D[..., 3] = S
     nodes, _ = orz.transformed_points(D, cell(120.0))
     got = mrz.nearest_sheared(torch.from_numpy(S).cuda(), X, Y, Z, cell(120.0), nodes).cpu().numpy()
     np.testing.assert_array_equal(got, S.ravel())
