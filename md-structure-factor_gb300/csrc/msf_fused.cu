@@ -521,7 +521,7 @@ static int launch_x_ct(const XCtArgs& a, cudaStream_t st) {
 }
 
 #define MSF_X_CASES(X) \
-  X(32, 32) X(64, 32) X(64, 16) X(128, 32) X(128, 16) X(256, 16) X(256, 8) X(512, 8) X(1024, 4)
+  X(32, 32) X(64, 32) X(64, 16) X(128, 32) X(128, 16) X(256, 32) X(256, 16) X(256, 8) X(512, 8) X(1024, 4)
 
 static int x_ct(const XCtArgs& a, int n0, int w, cudaStream_t st) {
 #define X(A, B) if (n0 == A && w == B) return launch_x_ct<A, B>(a, st);
@@ -530,9 +530,11 @@ static int x_ct(const XCtArgs& a, int n0, int w, cudaStream_t st) {
   return MSF_E_UNSUPPORTED;
 }
 
+// the requested tile width if it is instantiated for n0, else (0) the widest
+// tile of at most 4096 complex values (32 KB: two fit beside the plane FFT)
 int ct_x_width(int n0, int requested) {
   int best = 0;
-#define X(A, B) if (n0 == A && (requested == 0 ? B > best : B == requested)) best = B;
+#define X(A, B) if (n0 == A && (requested == 0 ? (B > best && A * B <= 4096) : B == requested)) best = B;
   MSF_X_CASES(X)
 #undef X
   return best;
@@ -744,8 +746,8 @@ int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int n
   return plane_ct(a, p->n1, p->n2, grids ? 1 : 0, p->n0, nframes, st);
 }
 
-int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf) {
-  if (p->xtma_ready) return xtma_batch(p, nframes, sf, st, buf);
+int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf, bool alone) {
+  if (p->xtma_ready) return xtma_batch(p, nframes, sf, st, buf, alone);
   XCtArgs a;
   a.C = ws_ptr<float2>(p, buf ? p->off_cplx2 : p->off_cplx);
   a.Vh = half_elems(p);

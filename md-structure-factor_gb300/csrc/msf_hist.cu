@@ -181,7 +181,8 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
       if (!s) s = fused_plane_batch(p, nullptr, kGridI32, nb, st, buf);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_plane[buf], st));
       if (!s) s = cuda_status(cudaStreamWaitEvent(p->side, p->ev_plane[buf], 0));
-      if (!s) s = fused_x_batch(p, nb, sf, p->side, buf);
+      // the last x pass of a chain has the SMs to itself
+      if (!s) s = fused_x_batch(p, nb, sf, p->side, buf, !cont && f + nb >= n_frames);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_x[buf], p->side));
     }
     if (cont && !s) {

@@ -287,7 +287,9 @@ int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weight
                        int flags, cudaStream_t st);
 int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st,
                       int buf = 0);
-int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf = 0);
+// alone: no plane FFT shares the SMs with this x pass (the last batch of a
+// chain, or a plan without overlap): the TMA x pass then fills every SM
+int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf = 0, bool alone = true);
 // destroys the streams/events a bind created (idempotent)
 void plan_release(msf_plan* p);
 // x pass with TMA tile loads (msf_xtma.cu); prepared at bind time
@@ -298,7 +300,7 @@ int smooth_stage_a(const msf_plan* p, const void* grids, int grid_kind, int nfra
 int smooth_stage_b(const msf_plan* p, int nframes, double* sf, cudaStream_t st);
 bool xtma_ok(int n0, int w);
 int xtma_prepare(msf_plan* p);
-int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf);
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf, bool alone);
 int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int layout, int64_t n_atoms,
                 const double* scale, int flags, int32_t* grid, cudaStream_t st);
 

@@ -190,7 +190,9 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
     while (w > 4 && nmax * w > 4096) w /= 2;
     while (w < 32 && nmax * w * 2 <= 4096) w *= 2;
   }
-  if ((size_t)(n[0] > n[1] ? n[0] : n[1]) * w > 4096) return MSF_E_UNSUPPORTED;
+  // (the generic engine's column tiles hold at most 4096 values; the fused
+  // chain checks its own instantiated widths)
+  if (variant != 3 && (size_t)(n[0] > n[1] ? n[0] : n[1]) * w > 4096) return MSF_E_UNSUPPORTED;
   p->tile_w = w;
   if (variant == 3) p->tile_w = ct_x_width(n[0], d->tile_w);
   int g = d->rows_per_block;

@@ -35,7 +35,7 @@ struct XTmaShape {
 };
 
 template <int N0, int W>
-__global__ void __launch_bounds__(256, (N0 <= 256 ? 3 : 1)) k_xpower_tma(const __grid_constant__ CUtensorMap map,
+__global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_xpower_tma(const __grid_constant__ CUtensorMap map,
                                                                        XTmaArgs a) {
   using S = XTmaShape<N0, W>;
   constexpr int NT = S::NT, EPT = S::EPT;
@@ -127,14 +127,20 @@ __global__ void __launch_bounds__(256, (N0 <= 256 ? 3 : 1)) k_xpower_tma(const _
         const int l = it % W, k1 = it / W;
         const bool ok = (ITEMS2 % NT == 0 || it < ITEMS2) && f0 + l < a.F;
         double* d = a.sf + (int64_t)k1 * a.F + f0 + l;
-        // all loads of the column first (independent), then the adds and stores
-        double old[A];
+        // in groups of 8: the group's loads first (independent), then the adds
+        // and stores (a whole column of FP64 values would not fit the
+        // register budget beside the accumulators)
+        constexpr int G8 = (W >= 16 && A > 8) ? 8 : A;
 #pragma unroll
-        for (int k2 = 0; k2 < A; ++k2) old[k2] = ok ? __ldcg(d + (int64_t)B * k2 * a.F) : 0.0;
+        for (int g = 0; g < A; g += G8) {
+          double old[G8];
 #pragma unroll
-        for (int k2 = 0; k2 < A; ++k2) {
-          if (ok) __stcg(d + (int64_t)B * k2 * a.F, old[k2] + (double)acc[j][k2]);
-          acc[j][k2] = 0.f;
+          for (int k2 = 0; k2 < G8; ++k2) old[k2] = ok ? __ldcg(d + (int64_t)B * (g + k2) * a.F) : 0.0;
+#pragma unroll
+          for (int k2 = 0; k2 < G8; ++k2) {
+            if (ok) __stcg(d + (int64_t)B * (g + k2) * a.F, old[k2] + (double)acc[j][g + k2]);
+            acc[j][g + k2] = 0.f;
+          }
         }
       }
     }
@@ -175,7 +181,7 @@ static EncodeTiledFn encode_fn() {
 }
 
 template <int N0, int W>
-static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs& a, cudaStream_t st) {
+static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs& a, cudaStream_t st, bool alone) {
   using S = XTmaShape<N0, W>;
   static int grid = 0, sms = 0;
   if (!grid) {
@@ -188,13 +194,15 @@ static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_xpower_tma<N0, W>, S::NT, S::SMEM);
     grid = (sms > 0 ? sms : 152) * (occ > 0 ? occ : 1);
   }
-  const int cap = p->overlap ? (sms > 0 ? sms : 152) : grid;
+  // beside a plane FFT: one CTA per SM (it co-resides with the plane CTA);
+  // alone: as many as fit
+  const int cap = (p->overlap && !alone) ? (sms > 0 ? sms : 152) : grid;
   const int g = a.ntiles < cap ? a.ntiles : cap;
   k_xpower_tma<N0, W><<<g, S::NT, S::SMEM, st>>>(*map, a);
   return launch_status();
 }
 
-#define MSF_XTMA_CASES(X) X(64, 32) X(128, 16) X(128, 32) X(256, 16) X(256, 8) X(512, 8)
+#define MSF_XTMA_CASES(X) X(64, 32) X(128, 16) X(128, 32) X(256, 32) X(256, 16) X(256, 8) X(512, 8)
 
 bool xtma_ok(int n0, int w) {
 #define X(A, B) if (n0 == A && w == B) return true;
@@ -227,7 +235,7 @@ int xtma_prepare(msf_plan* p) {
   return MSF_OK;
 }
 
-int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf) {
+int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf, bool alone) {
   XTmaArgs a;
   a.nframes = nframes;
   a.F = (int64_t)p->n1 * p->nh;
@@ -236,7 +244,7 @@ int xtma_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int 
   a.twx = ws_ptr<float2>(p, p->off_tw[0]);
   a.status = ws_ptr<int>(p, p->off_status);
   const CUtensorMap* map = reinterpret_cast<const CUtensorMap*>(p->xtma_map[buf]);
-#define X(A, B) if (p->n0 == A && p->tile_w == B) return launch_xtma<A, B>(p, map, a, st);
+#define X(A, B) if (p->n0 == A && p->tile_w == B) return launch_xtma<A, B>(p, map, a, st, alone);
   MSF_XTMA_CASES(X)
 #undef X
   return MSF_E_UNSUPPORTED;
