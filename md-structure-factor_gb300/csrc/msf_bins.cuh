@@ -53,6 +53,24 @@ __device__ __forceinline__ int bin_f32(float x, int n, float inv, const float* _
   return b;
 }
 
+// bin_f32 with the flo table in shared memory (plain loads) and the upper
+// edge fhi[n] passed by value
+__device__ __forceinline__ int bin_f32_tab(float x, int n, float inv, const float* flo, float hi_edge) {
+  const float lo_edge = flo[0];
+  int b = (int)(x * inv);
+  b = b < 0 ? 0 : (b > n - 1 ? n - 1 : b);
+  const float e0 = flo[b], e1 = flo[b + 1];
+  if (!(x >= lo_edge) || !(x <= hi_edge)) return -1;  // also drops NaN
+  if (x < e0) {
+    --b;
+    while (b > 0 && x < flo[b]) --b;
+  } else if (b < n - 1 && x >= e1) {
+    ++b;
+    while (b < n - 1 && x >= flo[b + 1]) ++b;
+  }
+  return b;
+}
+
 __device__ __forceinline__ int bin_f64(double x, int n, float inv, const double* __restrict__ e) {
   const double lo_edge = __ldg(e), hi_edge = __ldg(e + n);
   int b = (int)((float)x * inv);
@@ -138,6 +156,28 @@ __device__ __forceinline__ bool atom_bins(const DepArgs& a, int frame, int64_t i
       b2 = bin_f64(prep((double)v.z, s, 2, wrap, a.L2), a.n2, a.inv2, a.e2);
     }
   }
+  return (b0 >= 0) & (b1 >= 0) & (b2 >= 0);
+}
+
+// atom_bins for the FP32-search modes (0, 3) with the three flo tables in
+// shared memory (t: flo0 | flo1 | flo2, t_hi: the three fhi[n])
+template <int MODE>
+__device__ __forceinline__ bool atom_bins_tab(const DepArgs& a, int frame, int64_t i, const float* t,
+                                              const float* t_hi, int& b0, int& b1, int& b2, int& wgt) {
+  static_assert(MODE == 0 || MODE == 3, "FP32 search modes only");
+  float x, y, z;
+  if (MODE == 0) {
+    const float4 v = __ldg(static_cast<const float4*>(a.pos) + frame * a.frame_stride + i);
+    x = v.x; y = v.y; z = v.z;
+    wgt = __float2int_rn(v.w);
+  } else {
+    const float* r = static_cast<const float*>(a.pos) + frame * a.frame_stride + 3 * i;
+    wgt = __ldg(a.w + i);
+    x = __ldg(r + 0); y = __ldg(r + 1); z = __ldg(r + 2);
+  }
+  b0 = bin_f32_tab(x, a.n0, a.inv0, t, t_hi[0]);
+  b1 = bin_f32_tab(y, a.n1, a.inv1, t + a.n0 + 1, t_hi[1]);
+  b2 = bin_f32_tab(z, a.n2, a.inv2, t + a.n0 + a.n1 + 2, t_hi[2]);
   return (b0 >= 0) & (b1 >= 0) & (b2 >= 0);
 }
 

@@ -55,13 +55,27 @@ constexpr int kBucketIter = kBucketAtoms / kBucketThreads;
 
 template <int MODE>
 __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
+  constexpr bool kTab = MODE == 0 || MODE == 3;   // FP32 search: edge tables in shared memory
   __shared__ int hist[kMaxN + 1];
   __shared__ int warp_sum[kBucketThreads / 32];
+  __shared__ float tab[kTab ? 3 * (kMaxN + 1) : 1];
+  __shared__ float tab_hi[3];
   const int frame = blockIdx.y;
   const int blk = blockIdx.x;
   const int n0 = a.d.n0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i <= n0; i += kBucketThreads) hist[i] = 0;
+  if (kTab) {
+    const int n1 = a.d.n1, n2 = a.d.n2;
+    for (int i = tid; i <= n0; i += kBucketThreads) tab[i] = __ldg(a.d.flo0 + i);
+    for (int i = tid; i <= n1; i += kBucketThreads) tab[n0 + 1 + i] = __ldg(a.d.flo1 + i);
+    for (int i = tid; i <= n2; i += kBucketThreads) tab[n0 + n1 + 2 + i] = __ldg(a.d.flo2 + i);
+    if (tid == 0) {
+      tab_hi[0] = __ldg(a.d.fhi0 + n0);
+      tab_hi[1] = __ldg(a.d.fhi1 + n1);
+      tab_hi[2] = __ldg(a.d.fhi2 + n2);
+    }
+  }
   __syncthreads();
   const int64_t a0 = (int64_t)blk * kBucketAtoms + tid;
   int key[kBucketIter], vox[kBucketIter], wt[kBucketIter];
@@ -69,7 +83,11 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
   for (int it = 0; it < kBucketIter; ++it) {
     const int64_t i = a0 + it * kBucketThreads;
     int b0 = -1, b1 = 0, b2 = 0, w = 0;
-    const bool valid = (i < a.d.n_atoms) && atom_bins<MODE>(a.d, frame, i, b0, b1, b2, w);
+    bool valid;
+    if constexpr (kTab)
+      valid = (i < a.d.n_atoms) && atom_bins_tab<MODE>(a.d, frame, i, tab, tab_hi, b0, b1, b2, w);
+    else
+      valid = (i < a.d.n_atoms) && atom_bins<MODE>(a.d, frame, i, b0, b1, b2, w);
     key[it] = valid ? b0 : -1;
     vox[it] = b1 * a.d.n2 + b2;
     wt[it] = w;
