@@ -266,6 +266,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--tile-w", type=int, default=0)
     ap.add_argument("--no-overlap", action="store_true")
+    ap.add_argument("--staged-copy", action="store_true",
+                    help="e2e: copy host chunks to the device instead of the kernels reading pinned memory")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--stream-chunk", type=int, default=0,
@@ -316,7 +318,7 @@ def main():
         tuning["options"] = 1
     if not tuning:
         from mdsf import tune
-        tuning = tune.lookup(DIMS) or {"batch": 16}
+        tuning = tune.lookup(DIMS) or {}   # else the plan's defaults (bucketed chain, 64 frames per batch)
     plan = mdsf.get_plan(DIMS, box, device=dev, max_atoms=N_ATOMS, **tuning)
     st = torch.cuda.current_stream(dev)
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device=dev)
@@ -392,7 +394,7 @@ def main():
 
     def e2e_step():
         out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning,
-                                    stream_chunk=args.stream_chunk or None)
+                                    stream_chunk=args.stream_chunk or None, zero_copy=not args.staged_copy)
         if world > 1:
             dist.all_reduce(out)
         sf_h.copy_(out, non_blocking=True)
@@ -488,7 +490,9 @@ def main():
                          "chain_algorithmic_gbs": chain_gbs, "chain_frac": chain_gbs / peak},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(pos4_h.numel() * 4),
-                    "d2h_bytes_per_step": int(sf_h.numel() * 8)},
+                    "d2h_bytes_per_step": int(sf_h.numel() * 8),
+                    "h2d": ("chunked copies from pinned host memory on a side stream" if args.staged_copy
+                            else "kernels read the pinned host positions in place (mapped memory, NVLink-C2C)")},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
             "extras": extras,

@@ -788,6 +788,10 @@ extern "C" int msf_hist_bucket_grid(const msf_plan* p, int32_t layout, const voi
   if (n_atoms > 0 && (!pos || (layout != kLayoutF32x4 && !weights))) return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
   if (p->variant != 3) return MSF_E_UNSUPPORTED;
+  if (resolve_input(pos, reinterpret_cast<cudaStream_t>(stream)) ||
+      resolve_input(weights, reinterpret_cast<cudaStream_t>(stream)) ||
+      resolve_input(scale, reinterpret_cast<cudaStream_t>(stream)))
+    return MSF_E_INVALID;
   return bucket_grid(p, pos, weights, layout, n_atoms, scale, flags, grid,
                      reinterpret_cast<cudaStream_t>(stream));
 }

@@ -122,8 +122,9 @@ int msf_hist_grid_f32(const msf_plan* p, const void* pos_w, int64_t n_atoms, con
   if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && !pos_w)) return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
   if (check_flags(flags)) return MSF_E_INVALID;
-  return hist_deposit_batch(p, pos_w, nullptr, kLayoutF32x4, n_atoms, 1, n_atoms, scale, flags,
-                            grid, reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (resolve_input(pos_w, st) || resolve_input(scale, st)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos_w, nullptr, kLayoutF32x4, n_atoms, 1, n_atoms, scale, flags, grid, st);
 }
 
 int msf_hist_grid_f32xyz(const msf_plan* p, const float* pos, const int32_t* weights,
@@ -132,8 +133,9 @@ int msf_hist_grid_f32xyz(const msf_plan* p, const float* pos, const int32_t* wei
   if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && (!pos || !weights))) return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
   if (check_flags(flags)) return MSF_E_INVALID;
-  return hist_deposit_batch(p, pos, weights, kLayoutF32xyz, n_atoms, 1, 3 * n_atoms, scale, flags,
-                            grid, reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (resolve_input(pos, st) || resolve_input(weights, st) || resolve_input(scale, st)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos, weights, kLayoutF32xyz, n_atoms, 1, 3 * n_atoms, scale, flags, grid, st);
 }
 
 int msf_hist_grid_f64(const msf_plan* p, const double* pos, const int32_t* weights,
@@ -142,8 +144,9 @@ int msf_hist_grid_f64(const msf_plan* p, const double* pos, const int32_t* weigh
   if (!p || !grid || n_atoms < 0 || (n_atoms > 0 && (!pos || !weights))) return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
   if (check_flags(flags)) return MSF_E_INVALID;
-  return hist_deposit_batch(p, pos, weights, kLayoutF64, n_atoms, 1, 3 * n_atoms, scale, flags,
-                            grid, reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (resolve_input(pos, st) || resolve_input(weights, st) || resolve_input(scale, st)) return MSF_E_INVALID;
+  return hist_deposit_batch(p, pos, weights, kLayoutF64, n_atoms, 1, 3 * n_atoms, scale, flags, grid, st);
 }
 
 static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int layout,
@@ -157,6 +160,7 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
   const bool cont = flags & MSF_CONTINUE;
   flags &= ~MSF_CONTINUE;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (resolve_input(pos, st) || resolve_input(weights, st) || resolve_input(scale, st)) return MSF_E_INVALID;
   int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
   const int64_t fstride = layout == kLayoutF32x4 ? n_atoms : 3 * n_atoms;
   const size_t esize = layout == kLayoutF32x4 ? 4 * sizeof(float)
@@ -235,6 +239,7 @@ int msf_hist_batch_stages(msf_plan* p, int32_t stages, int32_t layout, const voi
   if ((stages & 4) && !sf) return MSF_E_INVALID;
   if (!p->bound) return MSF_E_NOT_BOUND;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (resolve_input(pos, st) || resolve_input(weights, st) || resolve_input(scale, st)) return MSF_E_INVALID;
   int32_t* grids = ws_ptr<int32_t>(p, p->off_grid);
   int s = MSF_OK;
   const bool bucketed = p->variant == 3;

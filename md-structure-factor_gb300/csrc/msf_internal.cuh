@@ -89,6 +89,40 @@ inline T* ws_ptr(const msf_plan* p, size_t off) { return reinterpret_cast<T*>(p-
 inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? MSF_OK : MSF_E_CUDA; }
 inline int launch_status() { return cuda_status(cudaGetLastError()); }
 
+// Input arrays the kernels read: device (or managed) memory as is; page-locked
+// host memory through its mapped device address (the kernels then read it in
+// place, on GB300 over NVLink-C2C, with no staging copy); pageable host
+// memory is refused (MSF_E_INVALID) instead of faulting in a kernel.  Not
+// queried while `st` is being captured into a graph (captured calls take
+// device pointers, as before).
+inline int resolve_input(const void*& ptr, cudaStream_t st) {
+  if (!ptr) return MSF_OK;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return MSF_OK;
+  }
+  if (cap != cudaStreamCaptureStatusNone) return MSF_OK;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return MSF_OK;
+  }
+  if (at.type == cudaMemoryTypeUnregistered) return MSF_E_INVALID;
+  if (at.type == cudaMemoryTypeHost) {
+    if (!at.devicePointer) return MSF_E_INVALID;
+    ptr = at.devicePointer;
+  }
+  return MSF_OK;
+}
+template <class T>
+inline int resolve_input(T*& ptr, cudaStream_t st) {
+  const void* v = ptr;
+  const int s = resolve_input(v, st);
+  ptr = static_cast<T*>(const_cast<void*>(v));
+  return s;
+}
+
 // ---------------------------------------------------------------- complex
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }

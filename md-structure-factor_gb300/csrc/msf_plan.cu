@@ -157,7 +157,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   memset(p, 0, sizeof(*p));
   p->n0 = n[0]; p->n1 = n[1]; p->n2 = n[2];
   p->nh = n[2] / 2 + 1;
-  p->batch = d->batch ? d->batch : 4;
+  p->batch = d->batch ? d->batch : 4;   // variant 3 default: below, once the variant is known
   for (int i = 0; i < 3; ++i) p->box[i] = d->box[i];
   for (int i = 0; i < 3; ++i) p->ax[i] = make_axis(n[i]);
   const int P = n[1] / 2;
@@ -178,6 +178,14 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   if (variant == 3 && !fused_ok) return MSF_E_UNSUPPORTED;
   if (variant == 4 && !smooth) return MSF_E_UNSUPPORTED;
   p->max_atoms = d->max_atoms;
+  if (variant == 3 && !d->batch) {
+    // the bucketed chain gains from long batches (fewer sf updates and bucket
+    // launches per frame, longer overlap): as many frames as keep its two
+    // spectrum buffers within 8 GiB, at most 64
+    const double spectra = 2.0 * (double)n[0] * n[1] * (n[2] / 2 + 1) * sizeof(float2);
+    const int64_t fit = (int64_t)((8.0 * 1024 * 1024 * 1024) / spectra);
+    p->batch = (int)(fit < 1 ? 1 : (fit > 64 ? 64 : fit));
+  }
   p->overlap = variant == 3 && !(d->options & MSF_PLAN_NO_OVERLAP);
   p->variant = variant;
   p->plane_smem = plane_smem;

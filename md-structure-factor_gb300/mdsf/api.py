@@ -90,13 +90,18 @@ def _launch_chain(plan, code, p, w, N, T, sc, flags, sf, st):
 
 
 def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False, mean=False,
-                     out=None, device=None, tuning=None, stream_chunk=None):
+                     out=None, device=None, tuning=None, stream_chunk=None, zero_copy=True):
     """Sum over frames of |rfftn(histogram)|^2, FP64, shape (n0, n1, n2//2+1).
 
     positions: (T, N, 3) or (N, 3) float32/float64, or (T, N, 4) float32 with
       the electron count in the 4th component (then ``weights`` is ignored).
-      Host arrays are streamed to the device in chunks of ``stream_chunk``
-      frames on a side stream (double-buffered, pinned memory), overlapping
+      Host arrays: with ``zero_copy`` (default) the kernels read them in place
+      from page-locked memory (one chain over all frames; on GB300 the reads
+      go over NVLink-C2C, no staging copy).  A pinned tensor passed in must
+      stay unchanged until the stream has finished the call; anything else
+      is first copied into pinned memory and the call waits for the kernels.
+      Without ``zero_copy`` they are copied to the device in chunks of
+      ``stream_chunk`` frames on a side stream (double-buffered), overlapping
       the copies with the kernels of the previous chunk.
     box: (3,) box edges, or (T, 3) per-frame boxes (frames are rescaled to
       the mean box as dens.py:46-62 does and binned in the mean box).
@@ -144,7 +149,15 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
         wptr = wd.data_ptr() if wd is not None else 0
         scp = sc.data_ptr() if sc is not None else 0
         chunk = int(stream_chunk or plan.batch)   # one batch: the first copy hides soonest
-        if not host or T <= chunk or N == 0:
+        if host and zero_copy and N > 0 and T > 0:
+            hp = pos if isinstance(pos, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(pos))
+            owned = not (hp.dtype == tdt and hp.is_contiguous() and hp.is_pinned())
+            if owned:
+                hp = hp.to(tdt).contiguous().pin_memory()
+            _launch_chain(plan, code, hp.data_ptr(), wptr, N, T, scp, flags, sf, st)
+            if owned:   # the kernels read hp in place: it must outlive them
+                torch.cuda.current_stream(device).synchronize()
+        elif not host or T <= chunk or N == 0:
             p = to_device(pos, device, tdt)
             _launch_chain(plan, code, p.data_ptr(), wptr, N, T, scp, flags, sf, st)
         else:

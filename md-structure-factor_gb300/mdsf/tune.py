@@ -47,18 +47,42 @@ def lookup(dims):
         return _read().get(_key(dims), {}).get("tuning")
 
 
+def _pow2(n):
+    return n >= 16 and n & (n - 1) == 0
+
+
+def _smooth(n):
+    if n == 512:
+        return True
+    if not 16 <= n <= 256:
+        return False
+    for f in (2, 3, 5):
+        while n % f == 0:
+            n //= f
+    return n == 1
+
+
 def candidates(dims):
+    """Bucketed chain (power-of-two axes, batches up to 64), the smooth
+    mixed-radix chain (2^a 3^b 5^c axes), and the generic engine's plane and
+    split variants with their tile widths and z rows per block."""
     n0, n1, n2 = dims
+    if all(_pow2(n) for n in dims):
+        for b in (16, 32, 64):
+            yield dict(variant=3, batch=b)
+    if all(_smooth(n) for n in dims):
+        for b in (4, 8, 16, 32):
+            yield dict(variant=4, batch=b)
     variants = [1, 2] if n1 % 2 == 0 else [2]
     tiles = [w for w in (4, 8, 16, 32) if max(n0, n1) * w <= 4096]
     rows = sorted({max(2, min(32, 2048 // n2)), max(2, min(32, 1024 // n2)), max(2, min(32, 4096 // n2))})
-    batches = [2, 4, 8, 16, 32]
+    batches = [4, 8, 16, 32]
     for v, w, b in itertools.product(variants, tiles, batches):
         for g in (rows if v == 2 else rows[:1]):
             yield dict(variant=v, tile_w=w, rows_per_block=g, batch=b)
 
 
-def time_config(dims, box, n_atoms, tuning, frames=16, reps=3, device=None):
+def time_config(dims, box, n_atoms, tuning, frames=None, reps=3, device=None):
     import torch
     from . import synth
     from .api import structure_factor
@@ -67,6 +91,8 @@ def time_config(dims, box, n_atoms, tuning, frames=16, reps=3, device=None):
         Plan(dims, box, device=device, **tuning)
     except Exception:
         return None
+    if frames is None:   # two batches at least, so that batching and overlap show
+        frames = max(16, 2 * int(tuning.get("batch", 4)))
     pos, _, w = synth.uniform_system(n_atoms, box, frames=frames, seed=17)
     p4 = torch.from_numpy(synth.pack_float4(pos, w)).cuda(device)
     out = torch.zeros((dims[0], dims[1], dims[2] // 2 + 1), dtype=torch.float64, device=p4.device)

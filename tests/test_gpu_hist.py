@@ -137,9 +137,36 @@ def test_host_streamed_chunks(chunk):
     pos, box, w = synth.uniform_system(4000, (2.0, 2.2, 1.8), frames=23, seed=31)
     ref = ohist.hist_sf(pos, box, w, (64, 64, 32))
     got = mdsf.structure_factor(pos.astype(np.float32), box, w, (64, 64, 32),
-                                tuning=dict(batch=4), stream_chunk=chunk).cpu().numpy()
+                                tuning=dict(batch=4), stream_chunk=chunk, zero_copy=False).cpu().numpy()
     assert mdsf.get_plan((64, 64, 32), box, max_atoms=4000, batch=4).tuning()["variant"] == "bucketed"
     assert rel_err(got, ref) < TOL
+
+
+@pytest.mark.parametrize("variant", [3, 4])
+def test_zero_copy_host_positions(variant):
+    """Pinned host positions read in place by the kernels give the same sf,
+    bit for bit, as the same call on a device copy; an unpinned array is
+    pinned first; pageable memory passed straight to the C ABI is refused
+    before any launch."""
+    from mdsf._lib import MsfError, c_p, call
+    pos, box, w = synth.uniform_system(5000, (2.0, 2.2, 1.8), frames=13, seed=41)
+    p4 = synth.pack_float4(pos.astype(np.float32), w)
+    dims = (64, 64, 32) if variant == 3 else (48, 60, 30)
+    tun = dict(batch=4, variant=variant)
+    dev = mdsf.structure_factor(torch.from_numpy(p4).cuda(), box, None, dims, tuning=tun)
+    pinned = torch.from_numpy(p4).pin_memory()
+    zc = mdsf.structure_factor(pinned, box, None, dims, tuning=tun)
+    torch.cuda.synchronize()
+    assert torch.equal(dev, zc)
+    zc2 = mdsf.structure_factor(p4, box, None, dims, tuning=tun)          # numpy: pinned copy
+    assert torch.equal(dev, zc2)
+    plan = mdsf.get_plan(dims, box, max_atoms=5000, **tun)
+    sf = torch.zeros(plan.half_shape, dtype=torch.float64, device="cuda")
+    with pytest.raises(MsfError):
+        call("msf_hist_sf_f32", plan.handle, c_p(p4.ctypes.data), 5000, 13, c_p(0), 0, c_p(sf.data_ptr()),
+             c_p(torch.cuda.current_stream().cuda_stream))
+    ref = ohist.hist_sf(pos.astype(np.float32), box, w, dims)
+    assert rel_err(zc.cpu().numpy(), ref) < TOL
 
 
 def test_continue_flag_equals_one_call():
