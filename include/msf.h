@@ -140,6 +140,12 @@ int msf_power_accum_f32(msf_plan* plan, const float* grids, int32_t n_grids, dou
  * (the reference's undivided sum, dens.py:318).
  *   pos_w:  (n_frames, n_atoms) float4 (x, y, z, w).
  *   scale:  NULL or (n_frames, 3) doubles (per-frame rescale factors).
+ * Input arrays (positions, weights, scale) of the deposit and chain calls
+ * may be device memory or page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister): the kernels then read the host array in place through
+ * its mapped address (on GB300 over NVLink-C2C), with no staging copy; it
+ * must stay unchanged until the stream has passed the call.  Pageable host
+ * memory is refused with MSF_E_INVALID before anything is launched.
  */
 int msf_hist_sf_f32(msf_plan* plan, const void* pos_w, int64_t n_atoms, int64_t n_frames,
                     const double* scale, int32_t flags, double* sf, msf_stream_t stream);
