@@ -266,8 +266,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--tile-w", type=int, default=0)
     ap.add_argument("--no-overlap", action="store_true")
-    ap.add_argument("--staged-copy", action="store_true",
-                    help="e2e: copy host chunks to the device instead of the kernels reading pinned memory")
+    ap.add_argument("--zero-copy", action="store_true",
+                    help="e2e: the kernels read the pinned host positions in place instead of staged copies")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--stream-chunk", type=int, default=0,
@@ -394,7 +394,7 @@ def main():
 
     def e2e_step():
         out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning,
-                                    stream_chunk=args.stream_chunk or None, zero_copy=not args.staged_copy)
+                                    stream_chunk=args.stream_chunk or None, zero_copy=args.zero_copy)
         if world > 1:
             dist.all_reduce(out)
         sf_h.copy_(out, non_blocking=True)
@@ -491,8 +491,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": int(pos4_h.numel() * 4),
                     "d2h_bytes_per_step": int(sf_h.numel() * 8),
-                    "h2d": ("chunked copies from pinned host memory on a side stream" if args.staged_copy
-                            else "kernels read the pinned host positions in place (mapped memory, NVLink-C2C)")},
+                    "h2d": ("kernels read the pinned host positions in place (mapped memory, NVLink-C2C)"
+                            if args.zero_copy else "chunked copies from pinned host memory on a side stream")},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
             "extras": extras,
