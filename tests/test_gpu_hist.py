@@ -155,10 +155,10 @@ def test_zero_copy_host_positions(variant):
     tun = dict(batch=4, variant=variant)
     dev = mdsf.structure_factor(torch.from_numpy(p4).cuda(), box, None, dims, tuning=tun)
     pinned = torch.from_numpy(p4).pin_memory()
-    zc = mdsf.structure_factor(pinned, box, None, dims, tuning=tun)
+    zc = mdsf.structure_factor(pinned, box, None, dims, tuning=tun, zero_copy=True)
     torch.cuda.synchronize()
     assert torch.equal(dev, zc)
-    zc2 = mdsf.structure_factor(p4, box, None, dims, tuning=tun)          # numpy: pinned copy
+    zc2 = mdsf.structure_factor(p4, box, None, dims, tuning=tun, zero_copy=True)   # numpy: pinned copy
     assert torch.equal(dev, zc2)
     plan = mdsf.get_plan(dims, box, max_atoms=5000, **tun)
     sf = torch.zeros(plan.half_shape, dtype=torch.float64, device="cuda")
