@@ -453,14 +453,20 @@ def main():
     peak, peak_kind = peaks()
     # DRAM bytes per launch of the dominant kernel from the committed ncu
     # capture of this workload (profiles/dram_traffic.txt), when it matches
-    traffic = None
+    # (a capture at another frame count per launch is scaled by the frames: the
+    # kernel's traffic is per frame plus nothing per launch)
+    traffic, traffic_note = None, None
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
-            for line in f:
-                fld = line.split()
-                if len(fld) == 4 and not line.startswith("#") and fld[0] == stage_names[dom] \
-                        and fld[1] == "x".join(map(str, DIMS)) and int(fld[2]) == kfull:
-                    traffic = int(fld[3])
+            rows = [ln.split() for ln in f if not ln.startswith("#")]
+        rows = [r for r in rows if len(r) == 4 and r[0] == stage_names[dom] and r[1] == "x".join(map(str, DIMS))]
+        exact = [r for r in rows if int(r[2]) == kfull]
+        if exact:
+            traffic = int(exact[0][3])
+        elif rows:
+            r = max(rows, key=lambda r: int(r[2]))
+            traffic = int(int(r[3]) * kfull / int(r[2]))
+            traffic_note = f"ncu capture at {r[2]} frames per launch, scaled to {kfull}"
     except (OSError, ValueError):
         pass
     chain_gbs = algorithmic_bytes_per_frame() * value / world / 1e9
@@ -484,7 +490,7 @@ def main():
                        "arithmetic": "int32 grid (FP32 binning exact vs FP64 edges), FP32 FFT, FP64 frame sum",
                        "tuning": plan.tuning(), "graph": world == 1, "parallelism": f"frames sharded x{world}"},
             "roofline": {"bound": "hbm", "kernel": stage_names[dom], "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "traffic_note": traffic_note,
                          "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "frames_per_launch": kfull,
                          "stage_ms_per_frame": {stage_names[s]: totals[s] / FRAMES for s in totals},
                          "chain_algorithmic_gbs": chain_gbs, "chain_frac": chain_gbs / peak},
