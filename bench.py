@@ -358,7 +358,7 @@ def main():
         run()
     torch.cuda.synchronize()
 
-    def timed(fn, steps):
+    def timed(fn, steps, join=()):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
@@ -367,6 +367,8 @@ def main():
         e0.record()
         for _ in range(steps):
             fn()
+        for js in join:   # the end event follows the work of these streams too
+            torch.cuda.current_stream().wait_stream(js)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -392,16 +394,26 @@ def main():
     # ---- e2e: public API from pinned host buffers, D2H of sf in the timed region
     sf_h = torch.empty(plan.half_shape, dtype=torch.float64).pin_memory()
 
+    d2h_stream = torch.cuda.Stream(dev)
+
     def e2e_step():
         out = mdsf.structure_factor(pos4_h, box, None, DIMS, device=dev, tuning=tuning,
                                     stream_chunk=args.stream_chunk or None, zero_copy=args.zero_copy)
         if world > 1:
             dist.all_reduce(out)
-        sf_h.copy_(out, non_blocking=True)
+        # the read-back of this step's sf on its own stream, so that the next
+        # step's kernels do not queue behind it (the timed region still ends
+        # with a device-wide synchronize)
+        done = torch.cuda.Event()
+        done.record()
+        with torch.cuda.stream(d2h_stream):
+            d2h_stream.wait_event(done)
+            sf_h.copy_(out, non_blocking=True)
+            out.record_stream(d2h_stream)
     for _ in range(2):
         e2e_step()
     torch.cuda.synchronize()
-    ms_e2e = timed(e2e_step, args.steps)
+    ms_e2e = timed(e2e_step, args.steps, join=(d2h_stream,))
     e2e_value = FRAMES * world * args.steps / (ms_e2e / 1000.0)
 
     # ---- roofline: each stage timed live with events around its launches
