@@ -266,6 +266,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--tile-w", type=int, default=0)
     ap.add_argument("--no-overlap", action="store_true")
+    ap.add_argument("--post-only", action="store_true",
+                    help="only the post-processing rows (radial, (r, z) histograms, nearest node)")
     ap.add_argument("--zero-copy", action="store_true",
                     help="e2e: the kernels read the pinned host positions in place instead of staged copies")
     ap.add_argument("--no-cpu", action="store_true")
@@ -301,6 +303,8 @@ def main():
         return run_batched_only(torch, dev, args)
     if args.stress_only:
         return run_stress_only(torch, dev, args)
+    if args.post_only:
+        return run_post_only(torch, dev, args)
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
@@ -603,6 +607,7 @@ def run_extras(mdsf, torch, dev, pos4, box, tuning, args):
     out["stress_512_frames_per_s"], out["stress_512_note"] = stress_512(torch, dev)
     out.update(radial_extra(torch, dev))
     out.update(rz_extra(torch, dev))
+    out.update(nearest_extra(torch, dev))
     out.update(gro_ingest())
     return out
 
@@ -663,6 +668,43 @@ def rz_extra(torch, dev, shape=(254, 254, 255), reps=3):
     return {"rz_voxels_per_s": shape[0] * shape[1] * shape[2] / dt,
             "rz_note": f"{shape} voxels, r/z edges = the x/z axes, theta = 120 deg cell, linear weights; wall time "
                        "per call incl. the D2H of the two histograms"}
+
+
+def nearest_extra(torch, dev, shape=(254, 254, 255), m=4_000_000, reps=3):
+    """Nearest node of the sheared 120-degree kgridplt grid (plot2d.py's
+    NearestNDInterpolator branch) for 4M random queries inside its extent."""
+    from mdsf import rz as mrz
+    from mdsf.api import plot_axes
+    X, Y, Z = plot_axes((shape[0] + 2, shape[1] + 2, (shape[2] + 3) // 2), np.array([160.0, 138.56, 80.0]))
+    th = 120 * np.pi / 180.0
+    ucell = np.array([[1, 0, 0], [np.cos(th), np.sin(th), 0], [0, 0, 1]])
+    g = torch.Generator(device=dev).manual_seed(5)
+    S = torch.rand(shape, dtype=torch.float64, device=dev, generator=g)
+    b = mrz.reciprocal_rows(ucell)
+    lo = np.array([X[0], Y[0], Z[0]]) @ np.abs(b) * 0.9
+    q = (torch.rand((m, 3), dtype=torch.float64, device=dev, generator=g) * 2 - 1) * torch.from_numpy(
+        np.abs(lo)).to(dev)
+    mrz.nearest_sheared(S, X, Y, Z, ucell, q)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        mrz.nearest_sheared(S, X, Y, Z, ucell, q)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    del S, q
+    return {"nearest_queries_per_s": m / dt,
+            "nearest_note": f"{m} queries on the {shape} grid in the 120-degree cell, wall time per call"}
+
+
+def run_post_only(torch, dev, args):
+    """The post-processing rows alone (radial_integrate, the (r, z)
+    histograms, the sheared-grid nearest node), for launch lists and ncu."""
+    out = {}
+    out.update(radial_extra(torch, dev))
+    out.update(rz_extra(torch, dev))
+    out.update(nearest_extra(torch, dev))
+    print(json.dumps({"metric": "post-processing rows on the 254x254x255 kgridplt", **out}))
+    return 0
 
 
 def gro_ingest(frames=8, atoms=N_ATOMS):
