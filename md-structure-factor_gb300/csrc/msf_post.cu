@@ -190,7 +190,7 @@ __device__ __forceinline__ int edge_bin(const double* __restrict__ e, int n, dou
   return (lo >= 1 && lo <= n - 1) ? lo - 1 : -1;
 }
 
-// One CTA per z-plane iz of the grid.  When the cell keeps b3 along z (the
+// CTAs over (z-plane iz, part of its (ix, iy) range).  When the cell keeps b3 along z (the
 // reference's cells), every voxel of the plane has the same pz and so the
 // same z bin: the plane's r histogram is summed in shared memory (FP64 sums,
 // u32 counts) and added to that z bin's row once.  A voxel whose z bin
@@ -203,6 +203,11 @@ __global__ void k_rz_hist(RzArgs a) {
   double* hs = reinterpret_cast<double*>(rz_sm);
   unsigned* cs = reinterpret_cast<unsigned*>(hs + nr);
   __shared__ int plane_bz;
+  // blockIdx.y splits the plane's (ix, iy) range over gridDim.y CTAs
+  const int64_t nxy_all = (int64_t)a.p0 * a.p1;
+  const int64_t chunk = (nxy_all + gridDim.y - 1) / gridDim.y;
+  const int64_t t0 = blockIdx.y * chunk;
+  const int64_t t1 = t0 + chunk < nxy_all ? t0 + chunk : nxy_all;
   for (int iz = blockIdx.x; iz < a.p2; iz += gridDim.x) {
     for (int i = threadIdx.x; i < nr; i += blockDim.x) { hs[i] = 0.0; cs[i] = 0u; }
     const double zv = __ldg(a.Z + iz);
@@ -214,8 +219,7 @@ __global__ void k_rz_hist(RzArgs a) {
     }
     __syncthreads();
     const int pbz = plane_bz;
-    const int64_t nxy = (int64_t)a.p0 * a.p1;
-    for (int64_t t = threadIdx.x; t < nxy; t += blockDim.x) {
+    for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
       const int ix = (int)(t / a.p1), iy = (int)(t % a.p1);
       const double xv = __ldg(a.X + ix), yv = __ldg(a.Y + iy);
       double p[3];
@@ -388,7 +392,14 @@ extern "C" int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, 
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_rz_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return MSF_E_CUDA;
-  k_rz_hist<<<p2, 256, smem, reinterpret_cast<cudaStream_t>(stream)>>>(a);
+  // z-planes x parts of each plane: enough CTAs to fill the GPU several times
+  const int64_t nxy = (int64_t)p0 * p1;
+  int parts = (int)((152LL * 16 + p2 - 1) / p2);
+  if (parts < 1) parts = 1;
+  if (parts > 64) parts = 64;
+  if ((int64_t)parts * 256 > nxy) parts = (int)((nxy + 255) / 256);
+  if (parts < 1) parts = 1;
+  k_rz_hist<<<dim3((unsigned)p2, (unsigned)parts), 256, smem, reinterpret_cast<cudaStream_t>(stream)>>>(a);
   return launch_status();
 }
 

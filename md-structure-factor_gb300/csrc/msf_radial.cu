@@ -129,55 +129,18 @@ __device__ __forceinline__ void bins_flush(const RadialBins& b, const double* hs
   if (bad) atomicOr(b.status, 1u);
 }
 
-// Adds each lane's (w, 1) to bin i of the shared histogram with one atomic
-// per run of equal bins in adjacent lanes (neighbouring voxels along z mostly
-// share a bin): a segmented inclusive scan over the warp by shuffles, then
-// the last lane of each run adds the run's sum and count.  All 32 lanes call
-// it; i < 0 contributes nothing.
-__device__ __forceinline__ void warp_runs_add(int i, double w, double* hs, unsigned* cs) {
-  constexpr unsigned kFull = 0xFFFFFFFFu;
-  const int lane = threadIdx.x & 31;
-  const int prev = __shfl_up_sync(kFull, i, 1);
-  const int next = __shfl_down_sync(kFull, i, 1);
-  bool head = lane == 0 || prev != i;
-  double v = i >= 0 ? w : 0.0;
-  unsigned n = i >= 0 ? 1u : 0u;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double vv = __shfl_up_sync(kFull, v, o);
-    const unsigned nn = __shfl_up_sync(kFull, n, o);
-    const int hh = __shfl_up_sync(kFull, (int)head, o);
-    if (lane >= o && !head) {
-      v += vv;
-      n += nn;
-      head = hh != 0;
-    }
-  }
-  if (i >= 0 && (lane == 31 || next != i)) {
-    atomicAdd(hs + i, v);
-    atomicAdd(cs + i, n);
-  }
-}
-
 __global__ void k_radial_bin_points(const double* __restrict__ D, int64_t nv, RadialBins b) {
   extern __shared__ __align__(16) unsigned char sm[];
   double* hs;
   unsigned* cs;
   const BinCtx c = bins_setup(b, sm, hs, cs);
   unsigned bad = 0u;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // warp-uniform trip count (every lane reaches the shuffles)
-  for (int64_t e0 = (int64_t)blockIdx.x * blockDim.x; e0 < nv; e0 += stride) {
-    const int64_t e = e0 + threadIdx.x;
-    int i = -1;
-    double w = 0.0;
-    if (e < nv) {
-      const double2 xy = __ldcs(reinterpret_cast<const double2*>(D + 4 * e));
-      const double2 zs = __ldcs(reinterpret_cast<const double2*>(D + 4 * e + 2));
-      i = c.index(r_of(xy.x, xy.y, zs.x), bad);
-      w = zs.y;
-    }
-    warp_runs_add(i, w, hs, cs);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nv; e += (int64_t)gridDim.x * blockDim.x) {
+    const double2 xy = __ldcs(reinterpret_cast<const double2*>(D + 4 * e));
+    const double2 zs = __ldcs(reinterpret_cast<const double2*>(D + 4 * e + 2));
+    const int i = c.index(r_of(xy.x, xy.y, zs.x), bad);
+    atomicAdd(hs + i, zs.y);
+    atomicAdd(cs + i, 1u);
   }
   bins_flush(b, hs, cs, bad);
 }
@@ -197,15 +160,10 @@ __global__ void k_radial_bin_grid(const double* __restrict__ S, int p0, int p1, 
     const int ix = (int)(row / p1), iy = (int)(row % p1);
     const unsigned short rxy = hadd(__ldg(hx + ix), __ldg(hy + iy));
     const double* s = S + row * p2;
-    for (int z0 = 0; z0 < p2; z0 += blockDim.x) {   // warp-uniform trip count
-      const int iz = z0 + threadIdx.x;
-      int i = -1;
-      double w = 0.0;
-      if (iz < p2) {
-        i = c.index(hadd(rxy, __ldg(hz + iz)), bad);
-        w = __ldcs(s + iz);
-      }
-      warp_runs_add(i, w, hs, cs);
+    for (int iz = threadIdx.x; iz < p2; iz += blockDim.x) {
+      const int i = c.index(hadd(rxy, __ldg(hz + iz)), bad);
+      atomicAdd(hs + i, __ldcs(s + iz));
+      atomicAdd(cs + i, 1u);
     }
   }
   bins_flush(b, hs, cs, bad);
