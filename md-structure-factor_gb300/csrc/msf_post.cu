@@ -262,10 +262,11 @@ __global__ void k_rz_hist(RzArgs a) {
 // cKDTree order).  Search: f = (q - o) Minv, the query's fractional index
 // in the lattice o + (i, j, k) M (M rows dX b1, dY b2, dZ b3, uniform-axis
 // steps); the node round(f) clamped to the grid is at distance rho, and
-// every node within rho of q has |i_a - f_a| <= rho * |Minv column a|, so
-// the box f_a -+ (rho |Minv_a| + 1) clamped to the grid holds the nearest
-// node (the +1 absorbs the axes' rounding).  Ties go to the lowest flat
-// index (C order).  A query with a NaN or infinite coordinate gets NaN
+// every node within rho of q has |i_a - f_a| <= (rho + delta) * |Minv
+// column a|, delta bounding how far a node lies from its uniform-lattice
+// model (the axes' deviation from equal steps), so that box, clamped to
+// the grid, holds the nearest node.  Ties go to the lowest flat index (C
+// order).  A query with a NaN or infinite coordinate gets NaN
 // (index -1) before any index arithmetic.
 struct NearestArgs {
   const double* S;
@@ -277,6 +278,7 @@ struct NearestArgs {
   double o[3];      // p(0, 0, 0)
   double minv[9];   // inverse of M (row major)
   double cn[3];     // Euclidean norms of the columns of minv
+  double delta;     // bound on |node - its uniform-lattice model|
   const double* q;  // (m, 3)
   int64_t m;
   double* out;
@@ -328,7 +330,7 @@ __global__ void k_nearest(NearestArgs a) {
     int lo[3], hi[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const double w = rho * a.cn[c] + 1.0;
+      const double w = (rho + a.delta) * a.cn[c] * (1.0 + 1e-9) + 1e-6;
       lo[c] = clamp_index(floor(f[c] - w), n[c]);
       hi[c] = clamp_index(ceil(f[c] + w), n[c]);
     }
@@ -365,6 +367,8 @@ extern "C" int msf_nearest_sheared(const double* S, int32_t p0, int32_t p1, int3
     a.cn[i] = lattice_host[21 + i];
     if (!(a.cn[i] >= 0.0) || a.cn[i] > 1e300) return MSF_E_INVALID;
   }
+  a.delta = lattice_host[24];
+  if (!(a.delta >= 0.0) || a.delta > 1e300) return MSF_E_INVALID;
   a.q = q; a.m = m; a.out = out; a.index = index;
   const int blocks = (int)((m + 127) / 128 < 152 * 16 ? (m + 127) / 128 : 152 * 16);
   k_nearest<<<blocks, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);

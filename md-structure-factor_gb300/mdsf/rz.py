@@ -132,16 +132,24 @@ def measure_intensity(kgridplt, box=(63, 73, 60, 40), full=False, device=None):
 
 
 def lattice_params(X, Y, Z, ucell):
-    """The 24 doubles msf_nearest_sheared takes: reciprocal rows, the first
-    node, the inverse of the step lattice and its column norms."""
+    """The 25 doubles msf_nearest_sheared takes: reciprocal rows, the first
+    node, the inverse of the step lattice, its column norms, and a bound on
+    how far a node lies from its uniform-lattice model (the axes' largest
+    deviations from equal steps, times |b_a|, summed, with a margin for the
+    rounding of the node arithmetic)."""
     X, Y, Z = (np.asarray(a, np.float64) for a in (X, Y, Z))
     b = reciprocal_rows(ucell)
     o = (X[0] * b[0] + Y[0] * b[1]) + Z[0] * b[2]
-    steps = [(a[-1] - a[0]) / (len(a) - 1) if len(a) > 1 else 1.0 for a in (X, Y, Z)]
+    axes = (X, Y, Z)
+    steps = [(a[-1] - a[0]) / (len(a) - 1) if len(a) > 1 else 1.0 for a in axes]
     M = np.vstack([steps[i] * b[i] for i in range(3)])
     minv = np.linalg.inv(M)
     cn = np.sqrt((minv ** 2).sum(axis=0))
-    return np.ascontiguousarray(np.concatenate([b.ravel(), o, minv.ravel(), cn]))
+    dev = sum(np.max(np.abs(a - (a[0] + np.arange(len(a)) * steps[i]))) * np.linalg.norm(b[i])
+              for i, a in enumerate(axes))
+    scale = sum(np.max(np.abs(a)) * np.linalg.norm(b[i]) for i, a in enumerate(axes))
+    delta = 2.0 * dev + 1e-12 * scale
+    return np.ascontiguousarray(np.concatenate([b.ravel(), o, minv.ravel(), cn, [delta]]))
 
 
 def nearest_sheared(S, X, Y, Z, ucell, points, return_index=False):

@@ -39,6 +39,28 @@ def test_nearest_matches_scipy(theta, shape, L):
     np.testing.assert_array_equal(got.cpu().numpy(), want)
 
 
+def test_nearest_with_unequal_axis_steps():
+    """Axes with unequal steps: the candidate box widens by their deviation
+    from the uniform lattice and still holds scipy's node."""
+    rng = np.random.default_rng(12)
+    shape = (24, 20, 17)
+    X, Y, Z = plot_axes((26, 22, 10), np.array([9.0, 8.0, 6.0]))
+    X = np.sort(X + rng.uniform(-0.3, 0.3, len(X)) * (X[1] - X[0]))
+    Z = np.sort(Z + rng.uniform(-0.2, 0.2, len(Z)) * (Z[1] - Z[0]))
+    S = rng.uniform(0, 1, shape)
+    D = np.zeros(shape + (4,))
+    D[..., 0], D[..., 1], D[..., 2] = X[:, None, None], Y[None, :, None], Z[None, None, :]
+    D[..., 3] = S
+    uc = cell(120.0)
+    nodes, _ = orz.transformed_points(D.copy(), uc)
+    lo, hi = nodes.min(axis=0), nodes.max(axis=0)
+    q = rng.uniform(lo, hi, (5000, 3))
+    want, widx = orz.nearest_sheared(D, uc, q)
+    got, gidx = mrz.nearest_sheared(torch.from_numpy(S).cuda(), X, Y, Z, uc, q, return_index=True)
+    np.testing.assert_array_equal(gidx.cpu().numpy(), widx)
+    np.testing.assert_array_equal(got.cpu().numpy(), want)
+
+
 def test_nearest_at_own_nodes_is_identity_and_nan_query():
     shape = (12, 10, 9)
     X, Y, Z = plot_axes((14, 12, 6), np.array([6.0, 5.0, 4.0]))
