@@ -190,68 +190,27 @@ __device__ __forceinline__ int edge_bin(const double* __restrict__ e, int n, dou
   return (lo >= 1 && lo <= n - 1) ? lo - 1 : -1;
 }
 
-// CTAs over (z-plane iz, part of its (ix, iy) range).  When the cell keeps b3 along z (the
-// reference's cells), every voxel of the plane has the same pz and so the
-// same z bin: the plane's r histogram is summed in shared memory (FP64 sums,
-// u32 counts) and added to that z bin's row once.  A voxel whose z bin
-// differs from the plane's first voxel (a general cell) goes straight to the
-// global histogram.  Sums and counts are those of numpy either way; only the
-// FP64 summation order differs.
 __global__ void k_rz_hist(RzArgs a) {
-  extern __shared__ __align__(16) unsigned char rz_sm[];
-  const int nr = a.nre - 1, nz = a.nze - 1;
-  double* hs = reinterpret_cast<double*>(rz_sm);
-  unsigned* cs = reinterpret_cast<unsigned*>(hs + nr);
-  __shared__ int plane_bz;
-  // blockIdx.y splits the plane's (ix, iy) range over gridDim.y CTAs
-  const int64_t nxy_all = (int64_t)a.p0 * a.p1;
-  const int64_t chunk = (nxy_all + gridDim.y - 1) / gridDim.y;
-  const int64_t t0 = blockIdx.y * chunk;
-  const int64_t t1 = t0 + chunk < nxy_all ? t0 + chunk : nxy_all;
-  for (int iz = blockIdx.x; iz < a.p2; iz += gridDim.x) {
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) { hs[i] = 0.0; cs[i] = 0u; }
-    const double zv = __ldg(a.Z + iz);
-    if (threadIdx.x == 0) {
-      // the z bin of voxel (0, 0, iz)
-      const double xv = __ldg(a.X), yv = __ldg(a.Y);
-      const double pz = __dadd_rn(__dadd_rn(__dmul_rn(xv, a.b[2]), __dmul_rn(yv, a.b[5])), __dmul_rn(zv, a.b[8]));
-      plane_bz = edge_bin(a.ze, a.nze, pz);
-    }
-    __syncthreads();
-    const int pbz = plane_bz;
-    for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      const int ix = (int)(t / a.p1), iy = (int)(t % a.p1);
-      const double xv = __ldg(a.X + ix), yv = __ldg(a.Y + iy);
-      double p[3];
+  const int64_t total = (int64_t)a.p0 * a.p1 * a.p2;
+  const int nz = a.nze - 1;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(e % a.p2);
+    const int64_t t = e / a.p2;
+    const int iy = (int)(t % a.p1), ix = (int)(t / a.p1);
+    const double xv = __ldg(a.X + ix), yv = __ldg(a.Y + iy), zv = __ldg(a.Z + iz);
+    double p[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        p[c] = __dadd_rn(__dadd_rn(__dmul_rn(xv, a.b[c]), __dmul_rn(yv, a.b[3 + c])), __dmul_rn(zv, a.b[6 + c]));
-      const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])));
-      const int br = edge_bin(a.re, a.nre, r);
-      const int bz = edge_bin(a.ze, a.nze, p[2]);
-      if (br < 0 || bz < 0) continue;
-      const int64_t e = t * a.p2 + iz;
-      const double w = a.mode == 0 ? interp3(a.S, a.p0, a.p1, a.p2, a.X, a.Y, a.Z, p[0], p[1], p[2]) : __ldg(a.S + e);
-      if (bz == pbz) {
-        atomicAdd(hs + br, w);
-        atomicAdd(cs + br, 1u);
-      } else {
-        const int64_t bin = (int64_t)br * nz + bz;
-        atomicAdd(a.hval + bin, w);
-        atomicAdd(a.hcount + bin, 1ull);
-      }
-    }
-    __syncthreads();
-    if (pbz >= 0) {
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        if (cs[i]) {
-          const int64_t bin = (int64_t)i * nz + pbz;
-          atomicAdd(a.hval + bin, hs[i]);
-          atomicAdd(a.hcount + bin, (unsigned long long)cs[i]);
-        }
-      }
-    }
-    __syncthreads();
+    for (int c = 0; c < 3; ++c)
+      p[c] = __dadd_rn(__dadd_rn(__dmul_rn(xv, a.b[c]), __dmul_rn(yv, a.b[3 + c])), __dmul_rn(zv, a.b[6 + c]));
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])));
+    const int br = edge_bin(a.re, a.nre, r);
+    const int bz = edge_bin(a.ze, a.nze, p[2]);
+    if (br < 0 || bz < 0) continue;
+    const double w = a.mode == 0 ? interp3(a.S, a.p0, a.p1, a.p2, a.X, a.Y, a.Z, p[0], p[1], p[2]) : __ldg(a.S + e);
+    const int64_t bin = (int64_t)br * nz + bz;
+    atomicAdd(a.hval + bin, w);
+    atomicAdd(a.hcount + bin, 1ull);
   }
 }
 
@@ -390,20 +349,9 @@ extern "C" int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, 
   a.re = r_edges; a.nre = n_r_edges; a.ze = z_edges; a.nze = n_z_edges;
   a.hval = hval;
   a.hcount = reinterpret_cast<unsigned long long*>(hcount);
-  // shared memory: the r histogram of one z-plane (FP64 sums + u32 counts)
-  const size_t smem = (size_t)(n_r_edges - 1) * 12;
-  if (smem > 200 * 1024) return MSF_E_UNSUPPORTED;
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_rz_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return MSF_E_CUDA;
-  // z-planes x parts of each plane: enough CTAs to fill the GPU several times
-  const int64_t nxy = (int64_t)p0 * p1;
-  int parts = (int)((152LL * 16 + p2 - 1) / p2);
-  if (parts < 1) parts = 1;
-  if (parts > 64) parts = 64;
-  if ((int64_t)parts * 256 > nxy) parts = (int)((nxy + 255) / 256);
-  if (parts < 1) parts = 1;
-  k_rz_hist<<<dim3((unsigned)p2, (unsigned)parts), 256, smem, reinterpret_cast<cudaStream_t>(stream)>>>(a);
+  const int64_t total = (int64_t)p0 * p1 * p2;
+  const int blocks = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
+  k_rz_hist<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
   return launch_status();
 }
 
