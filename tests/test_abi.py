@@ -112,3 +112,33 @@ def test_null_arguments():
     assert lib.msf_direct_fwd(None, 10, None, 10, 0, 1, None, None, None) == -1
     assert lib.msf_direct_bwd(None, 0, None, 0, 1, 1, None, None, None, None) == 0
     assert lib.msf_gauss_grid_f64(None, None, None, 0, None, 1, None, None, None) == -1
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of msf_plan_desc and msf_batch_system have the C
+    sizes and field offsets (compiled from include/msf.h with the host C
+    compiler)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    from conftest import ROOT
+    fields = {"msf_plan_desc": [f for f, _ in _lib.PlanDesc._fields_],
+              "msf_batch_system": [f for f, _ in _lib.BatchSystem._fields_]}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "msf.h"', "int main(void) {"]
+    for st, fs in fields.items():
+        lines.append('printf("%%zu\\n", sizeof(%s));' % st)
+        for f in fs:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (st, f))
+    lines.append("return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = []
+    for cls in (_lib.PlanDesc, _lib.BatchSystem):
+        want.append(C.sizeof(cls))
+        want += [getattr(cls, f).offset for f, _ in cls._fields_]
+    assert out == want
