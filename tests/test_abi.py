@@ -55,7 +55,7 @@ def create(**kw):
 @pytest.mark.parametrize("kw,code", [
     (dict(dims=(1, 64, 64)), -2), (dict(dims=(64, 2048, 64)), -2), (dict(box=(0.0, 1, 1)), -1),
     (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=5), -1),
-    (dict(tile_w=24), -1), (dict(deposit_block=100), -1), (dict(max_atoms=-1), -1),
+    (dict(tile_w=12), -1), (dict(deposit_block=100), -1), (dict(max_atoms=-1), -1),
     (dict(dims=(48, 48, 48), variant=3), -2),
 ])
 def test_plan_create_rejects(kw, code):
