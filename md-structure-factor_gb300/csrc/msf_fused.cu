@@ -539,8 +539,7 @@ static int launch_x_ct(const XCtArgs& a, cudaStream_t st) {
 }
 
 #define MSF_X_CASES(X) \
-  X(32, 32) X(64, 32) X(64, 16) X(128, 32) X(128, 16) X(256, 32) X(256, 16) X(256, 12) X(256, 8) X(512, 8) \
-  X(1024, 4)
+  X(32, 32) X(64, 32) X(64, 16) X(128, 32) X(128, 16) X(256, 32) X(256, 16) X(256, 8) X(512, 8) X(1024, 4)
 
 static int x_ct(const XCtArgs& a, int n0, int w, cudaStream_t st) {
 #define X(A, B) if (n0 == A && w == B) return launch_x_ct<A, B>(a, st);

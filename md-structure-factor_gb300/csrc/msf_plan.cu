@@ -152,7 +152,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   if (d->batch < 0 || d->batch > 256) return MSF_E_INVALID;
   if (d->variant < 0 || d->variant > 4) return MSF_E_INVALID;
   if (d->max_atoms < 0 || (d->options & ~MSF_PLAN_NO_OVERLAP)) return MSF_E_INVALID;
-  if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 12 && d->tile_w != 16 && d->tile_w != 32)
+  if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
   memset(p, 0, sizeof(*p));
   p->n0 = n[0]; p->n1 = n[1]; p->n2 = n[2];

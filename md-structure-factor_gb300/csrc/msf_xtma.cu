@@ -31,53 +31,51 @@ struct XTmaShape {
   static constexpr int BOX_ROWS = N0 <= 256 ? N0 : 256;
   static constexpr int NBOX = N0 / BOX_ROWS;
   static constexpr uint32_t TILE_BYTES = N0 * W * sizeof(float2);
-  // tile buffers in the ring: three for tiles of at most 24 KB (two loads in
-  // flight while one tile is transformed, and still room beside the plane
-  // FFT's CTA), else two
-  static constexpr int NB = TILE_BYTES <= 24 * 1024 ? 3 : 2;
-  static constexpr size_t SMEM = 1024 + NB * (size_t)TILE_BYTES + N0 * sizeof(float2);
+  static constexpr size_t SMEM = 1024 + 2 * (size_t)TILE_BYTES + N0 * sizeof(float2);
 };
 
 template <int N0, int W>
 __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_xpower_tma(const __grid_constant__ CUtensorMap map,
                                                                        XTmaArgs a) {
   using S = XTmaShape<N0, W>;
-  constexpr int NT = S::NT, EPT = S::EPT, NB = S::NB;
+  constexpr int NT = S::NT, EPT = S::EPT;
   static_assert(EPT * NT == N0 * W, "tile must split evenly over the threads");
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar[NB];
+  __shared__ __align__(8) uint64_t bar[2];
   __shared__ int abort_flag;
   // 1024-byte aligned tile buffers (TMA destination)
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   float2* buf0 = reinterpret_cast<float2*>(base);
-  float2* tw = buf0 + NB * N0 * W;
+  float2* buf1 = buf0 + N0 * W;
+  float2* tw = buf1 + N0 * W;
   const int tid = threadIdx.x;
   const int my_tiles = (a.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
   const int total = my_tiles > 0 ? my_tiles * a.nframes : 0;
   if (tid == 0) {
-#pragma unroll
-    for (int k = 0; k < NB; ++k) mbar_init(&bar[k], 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (int i = tid; i < N0; i += NT) tw[i] = a.twx[i];
   __syncthreads();
 
-  // item s (tile-major, then frame) lives in buffer s % NB
   auto issue = [&](int s) {
     const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
     const int frame = s % a.nframes;
-    float2* dst = buf0 + (s % NB) * N0 * W;
-    uint64_t* b = &bar[s % NB];
+    float2* dst = (s & 1) ? buf1 : buf0;
+    uint64_t* b = &bar[s & 1];
     mbar_expect_tx(b, S::TILE_BYTES);
 #pragma unroll
     for (int k = 0; k < S::NBOX; ++k)
       tma_load_2d(dst + k * S::BOX_ROWS * W, &map, tile * W, frame * N0 + k * S::BOX_ROWS, b);
   };
-  if (tid == 0)
-    for (int s = 0; s < NB && s < total; ++s) issue(s);
-  uint32_t phases = 0;   // bit k: parity of buffer k's next completion
+  if (tid == 0) {
+    if (total > 0) issue(0);
+    if (total > 1) issue(1);
+  }
+  uint32_t phase0 = 0, phase1 = 0;
   // pass-2 items (k1, column) owned by this thread; X[k1 + B*k2] power in acc
   constexpr int A = r2::Split2<N0>::A, B = r2::Split2<N0>::B;
   constexpr int ITEMS2 = B * W;
@@ -89,9 +87,9 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
     for (int k = 0; k < A; ++k) acc[j][k] = 0.f;
 
   for (int s = 0; s < total; ++s) {
-    const int b = s % NB;
+    const int b = s & 1;
     uint64_t* bb = &bar[b];
-    const uint32_t par = (phases >> b) & 1u;
+    const uint32_t par = b ? phase1 : phase0;
     long long spins = 0;
     while (!mbar_try_wait(bb, par)) {
       if (++spins > kWaitLimit) { atomicExch(&abort_flag, 1); break; }
@@ -101,8 +99,8 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
       if (tid == 0) atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
       break;
     }
-    phases ^= 1u << b;
-    float2* t = buf0 + b * N0 * W;
+    if (b) phase1 ^= 1u; else phase0 ^= 1u;
+    float2* t = b ? buf1 : buf0;
     r2::pass1<N0, W, W, 1, NT>(t, tw);
     __syncthreads();
 #pragma unroll
@@ -132,7 +130,7 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
         // in groups of 8: the group's loads first (independent), then the adds
         // and stores (a whole column of FP64 values would not fit the
         // register budget beside the accumulators)
-        constexpr int G8 = (W >= 16 && A > 8) ? 4 : ((W >= 12 && A > 8) ? 8 : A);
+        constexpr int G8 = (W >= 16 && A > 8) ? 8 : A;
 #pragma unroll
         for (int g = 0; g < A; g += G8) {
           double old[G8];
@@ -147,17 +145,16 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
       }
     }
     __syncthreads();   // every thread is done with buffer b
-    // refill it with item s + NB: NB - 1 copies run under each transform
-    if (tid == 0 && s + NB < total) {
+    if (tid == 0 && s + 2 < total) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(s + NB);
+      issue(s + 2);
     }
   }
   // leave no copy in flight into this CTA's shared memory (bounded)
   if (tid == 0 && abort_flag) {
-    for (int k = 0; k < NB; ++k) {
+    for (int k = 0; k < 2; ++k) {
       long long spins = 0;
-      while (!mbar_try_wait(&bar[k], (phases >> k) & 1u) && ++spins < kWaitLimit) {
+      while (!mbar_try_wait(&bar[k], k ? phase1 : phase0) && ++spins < kWaitLimit) {
       }
     }
   }
@@ -205,7 +202,7 @@ static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs
   return launch_status();
 }
 
-#define MSF_XTMA_CASES(X) X(64, 32) X(128, 16) X(128, 32) X(256, 32) X(256, 16) X(256, 12) X(256, 8) X(512, 8)
+#define MSF_XTMA_CASES(X) X(64, 32) X(128, 16) X(128, 32) X(256, 32) X(256, 16) X(256, 8) X(512, 8)
 
 bool xtma_ok(int n0, int w) {
 #define X(A, B) if (n0 == A && w == B) return true;
