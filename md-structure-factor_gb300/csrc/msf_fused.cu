@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
   __shared__ int warp_sum[kBucketThreads / 32];
   __shared__ float tab[kTab ? 3 * (kMaxN + 1) : 1];
   __shared__ float tab_hi[3];
+  __shared__ int2 stage[kBucketAtoms];   // the block's entries in sorted order
+  __shared__ int n_valid;
   const int frame = blockIdx.y;
   const int blk = blockIdx.x;
   const int n0 = a.d.n0;
@@ -128,17 +130,23 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
       if (loc[j]) atomicAdd(a.pcount + (int64_t)frame * n0 + idx, loc[j]);
     }
   }
-  if (tid == kBucketThreads - 1) bo[n0] = before + incl;
+  if (tid == kBucketThreads - 1) {
+    bo[n0] = before + incl;
+    n_valid = before + incl;
+  }
   __syncthreads();
   // placement: one independent shared-memory atomic per atom, so the
-  // iterations of a thread overlap instead of forming a chain
-  int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
+  // iterations of a thread overlap instead of forming a chain; the entries
+  // land in shared memory and leave in one coalesced copy of the segment
   int slot[kBucketIter];
 #pragma unroll
   for (int it = 0; it < kBucketIter; ++it) slot[it] = key[it] >= 0 ? atomicAdd(&hist[key[it]], 1) : -1;
 #pragma unroll
   for (int it = 0; it < kBucketIter; ++it)
-    if (slot[it] >= 0) bk[slot[it]] = make_int2(vox[it], wt[it]);
+    if (slot[it] >= 0) stage[slot[it]] = make_int2(vox[it], wt[it]);
+  __syncthreads();
+  int2* bk = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
+  for (int i = tid; i < n_valid; i += kBucketThreads) bk[i] = stage[i];
 }
 
 // ----------------------------------------------------------- plane (z, y)

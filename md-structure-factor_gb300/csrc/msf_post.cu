@@ -82,7 +82,9 @@ __device__ double interp3(const double* __restrict__ D, int p0, int p1, int p2,
 }
 
 // plot2d.py:236-263: theta = atan(sqrt(a^2 + b^2)/K); in-plane coordinates
-// times cos(theta), the third K*(1 - cos(theta)).
+// times cos(theta), the third K*(1 - cos(theta)).  cos(atan(t)) is computed
+// as 1/sqrt(1 + t^2), the same number up to rounding (a few ulps), at a
+// fraction of the FP64 cost of atan and cos.
 __global__ void k_ewald(const double* __restrict__ D, int p0, int p1, int p2,
                         const double* __restrict__ X, const double* __restrict__ Y,
                         const double* __restrict__ Z, double K, double* xy, double* xz,
@@ -100,7 +102,8 @@ __global__ void k_ewald(const double* __restrict__ D, int p0, int p1, int p2,
     const double A = plane == 2 ? __ldg(Y + ia) : __ldg(X + ia);
     const double Bv = plane == 0 ? __ldg(Y + ib) : __ldg(Z + ib);
     const double rho = sqrt(__dadd_rn(__dmul_rn(A, A), __dmul_rn(Bv, Bv)));
-    const double c = cos(atan(__ddiv_rn(rho, K)));
+    const double t = __ddiv_rn(rho, K);
+    const double c = __drcp_rn(__dsqrt_rn(__dadd_rn(1.0, __dmul_rn(t, t))));
     const double ua = __dmul_rn(A, c), ub = __dmul_rn(Bv, c), h = __dmul_rn(K, __dsub_rn(1.0, c));
     double v;
     if (plane == 0) { v = interp3(D, p0, p1, p2, X, Y, Z, ua, ub, h); xy[r] = v; }
