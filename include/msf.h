@@ -258,11 +258,13 @@ int msf_rz_hist(const double* S, int32_t p0, int32_t p1, int32_t p2, const doubl
  * (the non-orthorhombic branch; a KD-tree there): out[e] = S at the node
  * p(i,j,k) = X[i] b1 + Y[j] b2 + Z[k] b3 nearest q[e] (FP64 squared
  * Euclidean distance; ties to the lowest flat index; NaN for a NaN query).
- * lattice_host (25 doubles, host): b1 b2 b3 (rows), p(0,0,0), the inverse of
- * M = rows (dX b1, dY b2, dZ b3) with the mean axis steps, the norms of
- * that inverse's columns, and a bound on the distance of any node from its
- * position in that uniform lattice (sum over the axes of the largest
- * deviation from equal steps times |b_a|).  index (optional, device, m int64) receives the
+ * lattice_host (28 doubles, host): b1 b2 b3 (rows), p(0,0,0), the inverse of
+ * M = rows (dX b1, dY b2, dZ b3) with the mean axis steps, a bound on the
+ * distance of any node from its position in that uniform lattice (sum over
+ * the axes of the largest deviation from equal steps times |b_a|), and the
+ * upper Cholesky factor of M M^T (R00 R01 R02 R11 R12 R22).  The search
+ * enumerates the lattice points of the distance ball (Fincke-Pohst) inside
+ * the grid, so queries far outside the grid stay cheap.  index (optional, device, m int64) receives the
  * node's flat index.
  */
 int msf_nearest_sheared(const double* S, int32_t p0, int32_t p1, int32_t p2, const double* X, const double* Y,

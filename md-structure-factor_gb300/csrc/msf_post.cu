@@ -221,15 +221,20 @@ __global__ void k_rz_hist(RzArgs a) {
 // nodes are p(i, j, k) = X[i] b1 + Y[j] b2 + Z[k] b3 (numpy's order per
 // component, as k_rz_hist), the value at a query q is S at the node nearest
 // q in FP64 squared Euclidean distance ((dx^2 + dy^2) + dz^2, scipy's
-// cKDTree order).  Search: f = (q - o) Minv, the query's fractional index
-// in the lattice o + (i, j, k) M (M rows dX b1, dY b2, dZ b3, uniform-axis
-// steps); the node round(f) clamped to the grid is at distance rho, and
-// every node within rho of q has |i_a - f_a| <= (rho + delta) * |Minv
-// column a|, delta bounding how far a node lies from its uniform-lattice
-// model (the axes' deviation from equal steps), so that box, clamped to
-// the grid, holds the nearest node.  Ties go to the lowest flat index (C
-// order).  A query with a NaN or infinite coordinate gets NaN
-// (index -1) before any index arithmetic.
+// cKDTree order).  Search (Fincke-Pohst enumeration): in the uniform-lattice
+// model p = o + u M (u a real index vector, M rows dX b1, dY b2, dZ b3),
+// |q - p|^2 = (u - f) G (u - f)^T with f = (q - o) M^-1 and G = M M^T =
+// R^T R (R upper triangular), i.e. the sum over k of
+// (sum_{j >= k} R_kj (u_j - f_j))^2.  Starting from the node nearest round(f)
+// clamped to the grid, at distance rho, every node within rho lies within
+// rho + delta in the model (delta bounds a node's distance from its model
+// position: the axes' deviation from equal steps), so the enumeration of
+// index 2, then 1 given 2, then 0 given both, each interval intersected
+// with the grid, holds the nearest node; the radius shrinks as closer nodes
+// are found.  Queries outside the grid enumerate only the part of the ball
+// inside it.  Ties go to the lowest flat index (C order).  A query with a
+// NaN or infinite coordinate gets NaN (index -1) before any index
+// arithmetic.
 struct NearestArgs {
   const double* S;
   int p0, p1, p2;
@@ -239,8 +244,8 @@ struct NearestArgs {
   double b[9];      // rows b1, b2, b3
   double o[3];      // p(0, 0, 0)
   double minv[9];   // inverse of M (row major)
-  double cn[3];     // Euclidean norms of the columns of minv
   double delta;     // bound on |node - its uniform-lattice model|
+  double r[6];      // R00 R01 R02 R11 R12 R22
   const double* q;  // (m, 3)
   int64_t m;
   double* out;
@@ -268,7 +273,8 @@ __device__ __forceinline__ int clamp_index(double r, int n) {
 }
 
 __global__ void k_nearest(NearestArgs a) {
-  const int n[3] = {a.p0, a.p1, a.p2};
+  constexpr double kRel = 1.0 + 1e-9, kAbs = 1e-6;   // margins for the rounding of the bounds
+  const double R00 = a.r[0], R01 = a.r[1], R02 = a.r[2], R11 = a.r[3], R12 = a.r[4], R22 = a.r[5];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.m; e += (int64_t)gridDim.x * blockDim.x) {
     const double qx = __ldg(a.q + 3 * e), qy = __ldg(a.q + 3 * e + 1), qz = __ldg(a.q + 3 * e + 2);
     if (!(isfinite(qx) && isfinite(qy) && isfinite(qz))) {   // no finite nearest node: NaN
@@ -278,32 +284,47 @@ __global__ void k_nearest(NearestArgs a) {
     }
     const double d[3] = {qx - a.o[0], qy - a.o[1], qz - a.o[2]};
     double f[3];
-    int c0[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      f[c] = d[0] * a.minv[c] + d[1] * a.minv[3 + c] + d[2] * a.minv[6 + c];
-      c0[c] = clamp_index(rint(f[c]), n[c]);
-    }
+    for (int c = 0; c < 3; ++c) f[c] = d[0] * a.minv[c] + d[1] * a.minv[3 + c] + d[2] * a.minv[6 + c];
+    const int c0 = clamp_index(rint(f[0]), a.p0), c1 = clamp_index(rint(f[1]), a.p1),
+              c2 = clamp_index(rint(f[2]), a.p2);
     double p[3];
-    node_pos(a, c0[0], c0[1], c0[2], p);
+    node_pos(a, c0, c1, c2, p);
     double best = dist2(p, qx, qy, qz);
-    int64_t bi = ((int64_t)c0[0] * a.p1 + c0[1]) * a.p2 + c0[2];
-    const double rho = sqrt(best);
-    int lo[3], hi[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const double w = (rho + a.delta) * a.cn[c] * (1.0 + 1e-9) + 1e-6;
-      lo[c] = clamp_index(floor(f[c] - w), n[c]);
-      hi[c] = clamp_index(ceil(f[c] + w), n[c]);
-    }
-    for (int i = lo[0]; i <= hi[0]; ++i)
-      for (int j = lo[1]; j <= hi[1]; ++j)
-        for (int k = lo[2]; k <= hi[2]; ++k) {
-          node_pos(a, i, j, k, p);
+    int64_t bi = ((int64_t)c0 * a.p1 + c1) * a.p2 + c2;
+    double rad = sqrt(best) + a.delta;
+    const double w2 = rad * kRel / R22;
+    const int lo2 = clamp_index(floor(f[2] - w2 - kAbs), a.p2), hi2 = clamp_index(ceil(f[2] + w2 + kAbs), a.p2);
+    for (int i2 = lo2; i2 <= hi2; ++i2) {
+      const double u2 = (double)i2 - f[2];
+      const double t2 = R22 * u2;
+      const double r1sq = rad * rad * kRel - t2 * t2;
+      if (r1sq < 0.0) continue;
+      const double r1 = sqrt(r1sq);
+      const double cen1 = f[1] - R12 * u2 / R11;
+      const int lo1 = clamp_index(floor(cen1 - r1 / R11 - kAbs), a.p1);
+      const int hi1 = clamp_index(ceil(cen1 + r1 / R11 + kAbs), a.p1);
+      for (int i1 = lo1; i1 <= hi1; ++i1) {
+        const double u1 = (double)i1 - f[1];
+        const double t1 = R11 * u1 + R12 * u2;
+        const double r0sq = rad * rad * kRel - t2 * t2 - t1 * t1;
+        if (r0sq < 0.0) continue;
+        const double r0 = sqrt(r0sq);
+        const double cen0 = f[0] - (R01 * u1 + R02 * u2) / R00;
+        const int lo0 = clamp_index(floor(cen0 - r0 / R00 - kAbs), a.p0);
+        const int hi0 = clamp_index(ceil(cen0 + r0 / R00 + kAbs), a.p0);
+        for (int i0 = lo0; i0 <= hi0; ++i0) {
+          node_pos(a, i0, i1, i2, p);
           const double d2 = dist2(p, qx, qy, qz);
-          const int64_t fi = ((int64_t)i * a.p1 + j) * a.p2 + k;
-          if (d2 < best || (d2 == best && fi < bi)) { best = d2; bi = fi; }
+          const int64_t fi = ((int64_t)i0 * a.p1 + i1) * a.p2 + i2;
+          if (d2 < best || (d2 == best && fi < bi)) {
+            best = d2;
+            bi = fi;
+            rad = sqrt(best) + a.delta;   // the remaining intervals shrink with it
+          }
         }
+      }
+    }
     a.out[e] = __ldg(a.S + bi);
     if (a.index) a.index[e] = bi;
   }
@@ -325,12 +346,12 @@ extern "C" int msf_nearest_sheared(const double* S, int32_t p0, int32_t p1, int3
   for (int i = 0; i < 9; ++i) a.b[i] = lattice_host[i];
   for (int i = 0; i < 3; ++i) a.o[i] = lattice_host[9 + i];
   for (int i = 0; i < 9; ++i) a.minv[i] = lattice_host[12 + i];
-  for (int i = 0; i < 3; ++i) {
-    a.cn[i] = lattice_host[21 + i];
-    if (!(a.cn[i] >= 0.0) || a.cn[i] > 1e300) return MSF_E_INVALID;
-  }
-  a.delta = lattice_host[24];
+  a.delta = lattice_host[21];
   if (!(a.delta >= 0.0) || a.delta > 1e300) return MSF_E_INVALID;
+  for (int i = 0; i < 6; ++i) a.r[i] = lattice_host[22 + i];
+  // R's diagonal positive and finite (a non-singular lattice)
+  if (!(a.r[0] > 0.0 && a.r[3] > 0.0 && a.r[5] > 0.0) || !(a.r[0] < 1e300 && a.r[3] < 1e300 && a.r[5] < 1e300))
+    return MSF_E_INVALID;
   a.q = q; a.m = m; a.out = out; a.index = index;
   const int blocks = (int)((m + 127) / 128 < 152 * 16 ? (m + 127) / 128 : 152 * 16);
   k_nearest<<<blocks, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);

@@ -132,11 +132,12 @@ def measure_intensity(kgridplt, box=(63, 73, 60, 40), full=False, device=None):
 
 
 def lattice_params(X, Y, Z, ucell):
-    """The 25 doubles msf_nearest_sheared takes: reciprocal rows, the first
-    node, the inverse of the step lattice, its column norms, and a bound on
-    how far a node lies from its uniform-lattice model (the axes' largest
-    deviations from equal steps, times |b_a|, summed, with a margin for the
-    rounding of the node arithmetic)."""
+    """The 28 doubles msf_nearest_sheared takes: reciprocal rows (9), the
+    first node (3), the inverse of the step lattice M (rows dX b1, dY b2,
+    dZ b3; 9), a bound on how far a node lies from its uniform-lattice model
+    (the axes' largest deviations from equal steps times |b_a|, summed, with
+    a margin for the rounding of the node arithmetic; 1), and the upper
+    Cholesky factor R of M M^T = R^T R (R00 R01 R02 R11 R12 R22; 6)."""
     X, Y, Z = (np.asarray(a, np.float64) for a in (X, Y, Z))
     b = reciprocal_rows(ucell)
     o = (X[0] * b[0] + Y[0] * b[1]) + Z[0] * b[2]
@@ -144,12 +145,13 @@ def lattice_params(X, Y, Z, ucell):
     steps = [(a[-1] - a[0]) / (len(a) - 1) if len(a) > 1 else 1.0 for a in axes]
     M = np.vstack([steps[i] * b[i] for i in range(3)])
     minv = np.linalg.inv(M)
-    cn = np.sqrt((minv ** 2).sum(axis=0))
     dev = sum(np.max(np.abs(a - (a[0] + np.arange(len(a)) * steps[i]))) * np.linalg.norm(b[i])
               for i, a in enumerate(axes))
     scale = sum(np.max(np.abs(a)) * np.linalg.norm(b[i]) for i, a in enumerate(axes))
     delta = 2.0 * dev + 1e-12 * scale
-    return np.ascontiguousarray(np.concatenate([b.ravel(), o, minv.ravel(), cn, [delta]]))
+    R = np.linalg.cholesky(M @ M.T).T
+    r = [R[0, 0], R[0, 1], R[0, 2], R[1, 1], R[1, 2], R[2, 2]]
+    return np.ascontiguousarray(np.concatenate([b.ravel(), o, minv.ravel(), [delta], r]))
 
 
 def nearest_sheared(S, X, Y, Z, ucell, points, return_index=False):

@@ -31,6 +31,7 @@ def test_nearest_matches_scipy(theta, shape, L):
     lo, hi = nodes.min(axis=0), nodes.max(axis=0)
     span = hi - lo
     q = np.concatenate([rng.uniform(lo - 0.1 * span, hi + 0.1 * span, (4000, 3)),   # inside and around
+                        rng.uniform(lo - 1.5 * span, hi + 1.5 * span, (1000, 3)),   # far outside
                         nodes[rng.integers(0, len(nodes), 500)] + rng.normal(0, 1e-3, (500, 3)),
                         nodes[rng.integers(0, len(nodes), 200)]])                     # on nodes
     want, widx = orz.nearest_sheared(D, uc, q)
