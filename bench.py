@@ -696,7 +696,7 @@ def nearest_extra(torch, dev, shape=(254, 254, 255), m=4_000_000, reps=3):
     del S, q
     return {"nearest_queries_per_s": m / dt,
             "nearest_note": f"{m} queries inside the {shape} grid in the 120-degree cell, wall time per call "
-                            "(queries outside the grid cost more: the candidate box grows with their distance)"}
+                            "(Fincke-Pohst enumeration of the lattice points within the distance bound)"}
 
 
 def run_post_only(torch, dev, args):
