@@ -26,6 +26,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -65,7 +66,7 @@ class Clocks:
 
     def __init__(self, index=0):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(os.environ.get("MSF_BENCH_DIR", tempfile.gettempdir()), "clocks_bench.csv")
         self.index = index
         self.t0 = self.t1 = None
 
@@ -713,7 +714,6 @@ def run_post_only(torch, dev, args):
 def gro_ingest(frames=8, atoms=N_ATOMS):
     """Host trajectory ingest: the native multithreaded .gro reader on a
     synthetic 200k-atom, 8-frame file (3 decimals, cubic box)."""
-    import tempfile
     from mdsf import traj
     rng = np.random.default_rng(9)
     xyz = rng.uniform(0, 12.0, (atoms, 3))

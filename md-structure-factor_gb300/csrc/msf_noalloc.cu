@@ -4,7 +4,7 @@
 // Some hosts own every byte of device memory and forbid libraries to call
 // cudaMalloc once they are running: an MD engine that calls analysis hooks
 // between time steps from inside its own memory pool, a process started
-// under a hard per-process memory quota, or a C/Fortran driver that has no
+// under a hard per-process memory quota, or a C/Fortran host program that has no
 // allocator for device buffers beyond the arrays it already passes.  For
 // them msf_hist_sf_f32_noalloc runs the same kernels as msf_hist_sf_f32 but
 // keeps the plan on the stack and its workspace (FFT tables, bin edges, a

@@ -16,7 +16,7 @@ Modules (each function cites the reference file:line it follows):
 
 * :mod:`oracle.hist`   -- electron-weighted integer histogram on the box grid
   (``numpy.histogramdd`` semantics) -> rfftn -> |F|^2 -> FP64 sum over frames.
-  The reference has no histogram mode; this is the spec plain method
+  The reference has no histogram mode; this is the plain histogram method
   standing in for ``dens.py:283-318``.
 * :mod:`oracle.dens`   -- restatement of ``dens.compute_sf`` (Gaussian splat,
   padding fold with its corner quirk, rfftn, |F|^2, ``get_dplot``, ``kgrid``,
