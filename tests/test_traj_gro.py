@@ -168,3 +168,13 @@ def test_monoclinic_transform():
     got = traj.monoclinic(T, theta)
     assert got is T
     np.testing.assert_array_equal(got, want)
+
+
+def test_frames_without_atoms(tmp_path):
+    p = str(tmp_path / "empty.gro")
+    with open(p, "w") as f:
+        f.write("empty t=0\n    0\n   1.00000   1.00000   1.00000\n"
+                "empty t=1\n    0\n   2.00000   2.00000   2.00000\n")
+    x, d, nm = assert_same(p)
+    assert x.shape == (2, 0, 3) and len(nm) == 0
+    np.testing.assert_array_equal(d[:, 0], np.float32([10.0, 20.0]))
