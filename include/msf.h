@@ -376,6 +376,16 @@ size_t msf_noalloc_scratch_bytes(void);
  * vector lengths (float32 norms) * 10; names NULL or n_atoms x 8 bytes
  * (the first frame's atom names, NUL padded); threads 0 = all cores. */
 int msf_gro_scan(const char* path, int64_t* n_atoms, int64_t* n_frames);
+/* GROMACS .trr trajectories (XDR, single or double precision), the
+ * trajectory the reference CLI reads beside its .gro topology
+ * (main_gromacs.py:95-101 -> process_gro_mdtraj, load_traj.py:91-110).
+ * msf_trr_scan: atom and frame counts (MSF_E_UNSUPPORTED for a frame without
+ * positions or a changing atom count).  msf_trr_read: xyz (n_frames,
+ * n_atoms, 3) float32 Angstrom = float32(stored nm) * 10 in float32; box
+ * (n_frames, 3) the box vector lengths (float32 norms) * 10, 0 for a frame
+ * without a box; threads 0 = all cores. */
+int msf_trr_scan(const char* path, int64_t* n_atoms, int64_t* n_frames);
+int msf_trr_read(const char* path, int64_t n_atoms, int64_t n_frames, float* xyz, double* box, int32_t threads);
 int msf_gro_read(const char* path, int64_t n_atoms, int64_t n_frames, float* xyz, double* box, char* names,
                  int32_t threads);
 

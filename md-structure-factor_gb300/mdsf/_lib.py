@@ -95,6 +95,8 @@ SIGNATURES = {
     "msf_noalloc_scratch_bytes": (c_size, []),
     "msf_gro_scan": (c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "msf_gro_read": (c_int, [C.c_char_p, C.c_int64, C.c_int64, c_p, c_p, c_p, c_int]),
+    "msf_trr_scan": (c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "msf_trr_read": (c_int, [C.c_char_p, C.c_int64, C.c_int64, c_p, c_p, c_int]),
 }
 
 

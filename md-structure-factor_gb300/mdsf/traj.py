@@ -1,12 +1,12 @@
 """Trajectory ingest: GROMACS .gro trajectories into the reference's npz
 trajectory layout, and the monoclinic coordinate transform.
 
-Replaces load_traj.py's readers for .gro files -- ``process_gro_mdtraj``
+Replaces load_traj.py's readers for .gro and .trr files -- ``process_gro_mdtraj``
 (load_traj.py:91-110, which reads through mdtraj: coordinates nm -> Angstrom
 x10, unitcell lengths x10, then ``np.savez_compressed(out, dims, coords,
 name, mass, typ=name)``) and ``load_gro`` (load_traj.py:11-20, atom names) --
 and the transform of main_gromacs.py:204-207.  The parsing is native
-(``msf_gro_scan`` / ``msf_gro_read`` in libmsf, one host thread per group of
+(``msf_gro_*`` and ``msf_trr_*`` in libmsf, one host thread per group of
 frames); mdtraj is not needed.
 """
 from __future__ import annotations
@@ -62,6 +62,38 @@ def process_gro(gro_path, output_filename, threads=0):
     coords, dims, name = read_gro(gro_path, threads)
     mass = np.array([guess_mass(s) for s in name])
     np.savez_compressed(output_filename, dims=dims, coords=coords, name=name, mass=mass, typ=name)
+
+
+def scan_trr(path):
+    """(n_atoms, n_frames) of a .trr trajectory."""
+    na, nf = C.c_int64(), C.c_int64()
+    call("msf_trr_scan", str(path).encode(), C.byref(na), C.byref(nf))
+    return int(na.value), int(nf.value)
+
+
+def read_trr(path, threads=0):
+    """coords (T, N, 3) float32 Angstrom and dims (T, 3) float32 Angstrom
+    (box vector lengths) of a .trr trajectory."""
+    n, t = scan_trr(path)
+    xyz = np.empty((t, n, 3), np.float32)
+    box = np.empty((t, 3), np.float64)
+    call("msf_trr_read", str(path).encode(), n, t, c_p(xyz.ctypes.data), c_p(box.ctypes.data), int(threads))
+    return xyz, box.astype(np.float32)
+
+
+def process_gro_trr(topology_filename, trajectory_filename, output_filename, threads=0):
+    """load_traj.process_gro_mdtraj(top, traj, out) for the reference CLI's
+    pair (main_gromacs.py:95-101): atom names from the .gro topology,
+    coordinates and box lengths from the .trr (or a .gro) trajectory."""
+    names = read_gro(topology_filename, threads)[2]
+    if str(trajectory_filename).endswith(".gro"):
+        coords, dims, _ = read_gro(trajectory_filename, threads)
+    else:
+        coords, dims = read_trr(trajectory_filename, threads)
+    if coords.shape[1] != len(names):
+        raise ValueError("topology and trajectory have different atom counts")
+    mass = np.array([guess_mass(s) for s in names])
+    np.savez_compressed(output_filename, dims=dims, coords=coords, name=names, mass=mass, typ=names)
 
 
 def monoclinic(T, theta):

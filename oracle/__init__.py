@@ -25,6 +25,7 @@ Modules (each function cites the reference file:line it follows):
 * :mod:`oracle.direct` -- FP64 direct-sum S(q) and its analytic gradient.
 * :mod:`oracle.cyl`    -- the cylindrical (r, z) average of ``plot2d.PLOT_RAD_NEW``.
 * :mod:`oracle.gro`    -- .gro trajectory ingest (``load_traj.py``).
+* :mod:`oracle.trr`    -- .trr trajectory frames (the CLI's trajectory format).
 
 Pinning: ``tests/golden/*.npz`` hold outputs of the reference's own
 ``dens.compute_sf`` and ``plot2d.Plot_Ewald_Sphere_Correction`` run in the
