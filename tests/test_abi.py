@@ -142,3 +142,12 @@ def test_ctypes_structs_match_the_header(tmp_path):
         want.append(C.sizeof(cls))
         want += [getattr(cls, f).offset for f, _ in cls._fields_]
     assert out == want
+
+
+def test_integration_map_names_every_entry_point():
+    """Every function of include/msf.h has its row in INTEGRATION.md's entry
+    point map (what it replaces in the reference)."""
+    h = open(os.path.join(ROOT, "include", "msf.h")).read()
+    names = sorted(set(re.findall(r"\b(msf_[a-z0-9_]+)\s*\(", h)))
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    assert [n for n in names if n not in doc] == []
