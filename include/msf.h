@@ -81,15 +81,23 @@ typedef struct msf_plan_desc {
   int32_t deposit_block;  /* threads per deposit block: 0 auto */
   int64_t max_atoms;      /* atoms per frame the chain may be called with (sizes the per-plane
                              atom buckets of variant 3); 0 = no buckets */
-  int32_t options;        /* MSF_PLAN_NO_OVERLAP: keep variant 3 on the caller's stream only */
+  int32_t options;        /* MSF_PLAN_NO_OVERLAP: keep variant 3 on the caller's stream only;
+                             MSF_PLAN_DIAG_STALL: diagnostic (below) */
 } msf_plan_desc;
 
 /* msf_plan_desc.options.  By default a variant-3 plan double-buffers its
  * spectra and msf_plan_bind creates one internal stream and four events:
  * the x pass of each batch then runs on that stream, overlapped with the
  * plane FFT of the next batch (forked from and joined back to the caller's
- * stream, so the calls stay stream-ordered and graph-capturable). */
-enum { MSF_PLAN_NO_OVERLAP = 1 };
+ * stream, so the calls stay stream-ordered and graph-capturable).
+ * The kernels' waits on their own asynchronous copies are bounded (2^26
+ * polls of the mbarrier): a wait that runs out latches MSF_E_TIMEOUT, the
+ * kernel returns, and msf_plan_status() reports it.  MSF_PLAN_DIAG_STALL is
+ * a diagnostic for that error path: the variant-3 plane kernel arms its
+ * first wait for 16 bytes that no copy delivers and gives up after 2^14
+ * polls, so every call on the plan ends in MSF_E_TIMEOUT (its sf is not
+ * valid) while the context stays usable. */
+enum { MSF_PLAN_NO_OVERLAP = 1, MSF_PLAN_DIAG_STALL = 2 };
 
 int msf_plan_create(msf_plan** plan, const msf_plan_desc* desc);
 int msf_plan_destroy(msf_plan* plan);
@@ -348,21 +356,36 @@ int msf_batch_destroy(msf_batch* batch);
  * from inside its own memory pool, or a process under a hard device-memory
  * quota).  Same result as msf_hist_sf_f32 (sf += the frame sum of
  * |rfftn(histogram)|^2; pos_w device float4 (n_frames, n_atoms); box_host 3
- * doubles in host memory), but the plan lives on the stack and the
- * workspace is a fixed 32 MiB array inside the library image, which every
- * GPU that loads libmsf.so holds until the process exits
- * (msf_noalloc_scratch_bytes()).  Grids whose workspace does not fit
- * (batch 1: 4*n0*n1*n2 + 8*n0*n1*(n2/2+1) bytes plus small tables; e.g.
- * 128^3 fits, 256x256x128 does not) return MSF_E_WORKSPACE.  Nothing is
- * allocated or freed.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and may load the module: make that
- * first call before any stream capture.  Every call reuses the same array
- * and re-initialises it, so calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller. */
+ * doubles in host memory; flags 0 or MSF_WRAP -- MSF_CONTINUE is refused with
+ * MSF_E_INVALID, one call is one whole chain), but the plan lives on the
+ * stack and the workspace is a fixed 32 MiB array inside the library image,
+ * which every GPU that loads libmsf.so holds until the process exits
+ * (msf_noalloc_scratch_bytes()).  Grids whose batch-1 workspace does not fit
+ * in it (e.g. 256x256x128 on the non-bucketed variants) return
+ * MSF_E_WORKSPACE.  No call allocates or frees anything, with one
+ * exception: loading.  The CUDA runtime loads the library's module (which
+ * holds the 32 MiB array) and each kernel's code on first use, and that
+ * takes device memory; so call msf_noalloc_init() once per device and grid
+ * shape, while the host still allows allocation and before any stream
+ * capture; calls on that shape then allocate nothing.  Every call reuses the
+ * same array and re-initialises its tables, so calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialised by the caller.
+ * Errors the kernels detect (MSF_E_TIMEOUT of a bounded wait) stay latched in
+ * the array until msf_noalloc_status() reads them: check it after a call
+ * whose result matters. */
 int msf_hist_sf_f32_noalloc(const void* pos_w, int64_t n_atoms, int64_t n_frames,
                             const double* box_host, int32_t n0, int32_t n1, int32_t n2,
                             int32_t flags, double* sf, msf_stream_t stream);
 size_t msf_noalloc_scratch_bytes(void);
+/* Loads what msf_hist_sf_f32_noalloc needs on the current device for grid
+ * (n0, n1, n2): looks up the array's device address and runs the chain once,
+ * with and without MSF_WRAP, on one placeholder atom that every binning drops
+ * (sf += 0: sf is a device FP64 (n0, n1, n2/2+1) array, left unchanged). */
+int msf_noalloc_init(int32_t n0, int32_t n1, int32_t n2, double* sf, msf_stream_t stream);
+/* Synchronises `stream`, returns the error latched by the allocation-free
+ * calls on the current device since the last check (MSF_OK if none) and
+ * clears it. */
+int msf_noalloc_status(msf_stream_t stream);
 
 /* ---------------------------------------------- trajectory ingest (host)
  * GROMACS .gro trajectories (one or more frames, fixed columns), read on the

@@ -253,15 +253,18 @@ __global__ void __launch_bounds__(kXThreads) k_xpower(XArgs a) {
         acc[i] = fmaf(v.x, v.x, fmaf(v.y, v.y, acc[i]));
       }
     }
-  }
+    if (b == a.nframes - 1 || b % kPowerFlush == kPowerFlush - 1) {
 #pragma unroll
-  for (int i = 0; i < kXEpt; ++i) {
-    const int e = threadIdx.x + i * kXThreads;
-    if (e < nel) {
-      const int x = e / W, w = e % W;
-      if (w < weff) {
-        double* d = a.sf + (int64_t)x * a.F + f0 + w;
-        *d = *d + (double)acc[i];
+      for (int i = 0; i < kXEpt; ++i) {
+        const int e = threadIdx.x + i * kXThreads;
+        if (e < nel) {
+          const int x = e / W, w = e % W;
+          if (w < weff) {
+            double* d = a.sf + (int64_t)x * a.F + f0 + w;
+            *d = *d + (double)acc[i];
+          }
+        }
+        acc[i] = 0.f;
       }
     }
   }

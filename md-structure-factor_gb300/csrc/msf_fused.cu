@@ -22,7 +22,8 @@
 //                    never goes to global memory.
 //   k_xpower_tma     (msf_xtma.cu; k_xpower_ct without TMA) x-FFT of W spectrum
 //                    columns for every frame of the batch, |F|^2 summed over
-//                    the batch in FP32, one FP64 RMW of sf.
+//                    the batch in FP32, one FP64 RMW of sf every kPowerFlush
+//                    frames and after the last.
 // All FFT lengths are template constants (msf_r2.cuh, msf_ct.cuh).
 #include <math.h>
 
@@ -162,6 +163,8 @@ struct PlaneCtArgs {
   const int* poff;
   int64_t pstride;
   int* status;
+  long long wait_limit;   // bounded-wait limit (polls)
+  int stall;          // MSF_PLAN_DIAG_STALL: arm the first wait for a copy never issued
   // output
   float2* C;
   int64_t Vh;
@@ -314,8 +317,11 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
 // kPlanePrefetch*NT of them into shared memory with one cp.async.bulk copy
 // tracked by an mbarrier, issued before the FFT of the previous plane, so the
 // copy runs under that FFT.  Entries beyond the staged part are read from
-// global memory at deposit time.  The wait is bounded: on timeout the kernel
-// latches MSF_E_TIMEOUT in the plan status word and returns.
+// global memory at deposit time.  The wait is bounded (a.wait_limit polls):
+// on timeout the kernel latches MSF_E_TIMEOUT in the plan status word and
+// returns.  With a.stall (the plan's diagnostic option) the
+// first wait expects 16 bytes that no copy delivers, so it runs out: the
+// error path can be tested without any fault.
 constexpr int kPlanePrefetch = 2;
 
 template <int N1, int N2>
@@ -355,6 +361,10 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     return make_int2(po[0], po[1] - po[0]);
   };
   auto issue = [&](int item, int2 r) {
+    if (a.stall) {
+      mbar_expect_tx(bar, 16);
+      return;
+    }
     const int ns = r.y < CAP ? r.y : CAP;
     mbar_expect_tx(bar, (uint32_t)ns * sizeof(int2));
     if (ns > 0) bulk_load(staged, a.pbucket + (int64_t)(item / a.n0) * a.pstride + r.x, ns * sizeof(int2), bar);
@@ -382,7 +392,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
     long long spins = 0;
     while (!mbar_try_wait(bar, phase)) {
-      if (++spins > kWaitLimit) { atomicExch(ctl + 2, 1); break; }
+      if (++spins > a.wait_limit) { atomicExch(ctl + 2, 1); break; }
     }
     __syncthreads();
     if (ctl[2]) {
@@ -417,7 +427,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
   // leave no copy in flight into this CTA's shared memory (bounded)
   if (tid == 0 && ctl[2]) {
     long long spins = 0;
-    while (!mbar_try_wait(bar, phase) && ++spins < kWaitLimit) {
+    while (!mbar_try_wait(bar, phase) && ++spins < a.wait_limit) {
     }
   }
 }
@@ -468,14 +478,17 @@ __global__ void __launch_bounds__(XShape<N0, W>::NT) k_xpower_ct(XCtArgs a) {
       const float2 v = tile[threadIdx.x + i * NT];
       acc[i] = fmaf(v.x, v.x, fmaf(v.y, v.y, acc[i]));
     }
-  }
+    if (b == a.nframes - 1 || b % kPowerFlush == kPowerFlush - 1) {
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const int e = threadIdx.x + i * NT;
-    const int x = e / W, w = e % W;
-    if (w < weff) {
-      double* d = a.sf + (int64_t)x * a.F + f0 + w;
-      *d = *d + (double)acc[i];
+      for (int i = 0; i < EPT; ++i) {
+        const int e = threadIdx.x + i * NT;
+        const int x = e / W, w = e % W;
+        if (w < weff) {
+          double* d = a.sf + (int64_t)x * a.F + f0 + w;
+          *d = *d + (double)acc[i];
+        }
+        acc[i] = 0.f;
+      }
     }
   }
 }
@@ -760,6 +773,8 @@ static PlaneCtArgs plane_args(const msf_plan* p) {
   a.poff = ws_ptr<int>(p, p->off_poff);
   a.pstride = p->pstride;
   a.status = ws_ptr<int>(p, p->off_status);
+  a.wait_limit = p->wait_limit;
+  a.stall = p->diag_stall;
   return a;
 }
 

@@ -15,6 +15,13 @@ namespace msf {
 constexpr int kMaxStages = 12;
 constexpr int kMaxN = 1024;      // largest supported axis length
 constexpr int kStatusWords = 16; // device status block (int32)
+// The x passes sum |F|^2 over the frames of a batch in FP32 registers and add
+// that partial sum to the FP64 sf every kPowerFlush frames (and after the
+// batch's last frame).  A recursive FP32 sum of k positive terms is within
+// (k-1)*2^-24 of the exact sum relative to itself, so 32 frames bound the
+// in-register error by 1.9e-6 of each voxel's value, whatever the batch size
+// (plans accept up to 256 frames per batch); every longer sum is FP64.
+constexpr int kPowerFlush = 32;
 constexpr int kBucketAtoms = 2048; // atoms per bucketing block (bucketed variant)
 
 // Device status words (latched by kernels, read by msf_plan_status).
@@ -76,6 +83,13 @@ struct msf_plan {
   // a chain continued over several calls (MSF_CONTINUE): batches issued so
   // far, for the spectrum-buffer parity and the reuse waits; 0 when joined
   int64_t chain_k;
+  // bounded device waits: the plane kernel's poll limit, and the diagnostic
+  // option that makes its wait run out
+  long long wait_limit;
+  int diag_stall;
+  // msf_plan_bind leaves the status word as it is (the allocation-free entry
+  // point re-binds its plan on every call; its errors stay latched until read)
+  int keep_status;
 };
 
 namespace msf {

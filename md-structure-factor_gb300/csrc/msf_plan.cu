@@ -12,6 +12,7 @@
 #include <new>
 
 #include "msf_internal.cuh"
+#include "msf_tma.cuh"
 
 namespace msf {
 
@@ -55,7 +56,7 @@ struct TabArgs {
   double* edges;          // concatenated (n0+1, n1+1, n2+1)
   float* flo;
   float* fhi;
-  int* status;
+  int* status;    // zeroed unless NULL
 };
 
 __global__ void k_init_tables(TabArgs a) {
@@ -89,7 +90,8 @@ __global__ void k_init_tables(TabArgs a) {
     }
     base += n + 1;
   }
-  for (int i = gt; i < kStatusWords; i += gs) a.status[i] = 0;
+  if (a.status)
+    for (int i = gt; i < kStatusWords; i += gs) a.status[i] = 0;
 }
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -151,7 +153,7 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
     if (!(d->box[i] > 0.0) || !isfinite(d->box[i])) return MSF_E_INVALID;
   if (d->batch < 0 || d->batch > 256) return MSF_E_INVALID;
   if (d->variant < 0 || d->variant > 4) return MSF_E_INVALID;
-  if (d->max_atoms < 0 || (d->options & ~MSF_PLAN_NO_OVERLAP)) return MSF_E_INVALID;
+  if (d->max_atoms < 0 || (d->options & ~(MSF_PLAN_NO_OVERLAP | MSF_PLAN_DIAG_STALL))) return MSF_E_INVALID;
   if (d->tile_w != 0 && d->tile_w != 4 && d->tile_w != 8 && d->tile_w != 16 && d->tile_w != 32)
     return MSF_E_INVALID;
   memset(p, 0, sizeof(*p));
@@ -187,6 +189,8 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
     p->batch = (int)(fit < 1 ? 1 : (fit > 64 ? 64 : fit));
   }
   p->overlap = variant == 3 && !(d->options & MSF_PLAN_NO_OVERLAP);
+  p->diag_stall = (d->options & MSF_PLAN_DIAG_STALL) ? 1 : 0;
+  p->wait_limit = p->diag_stall ? kDiagWaitLimit : kWaitLimit;
   p->variant = variant;
   p->plane_smem = plane_smem;
   p->plane_threads = (n[2] * P >= 8192) ? 512 : 256;
@@ -275,7 +279,7 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
   a.edges = ws_ptr<double>(p, p->off_edges_d);
   a.flo = ws_ptr<float>(p, p->off_edges_flo);
   a.fhi = ws_ptr<float>(p, p->off_edges_fhi);
-  a.status = ws_ptr<int>(p, p->off_status);
+  a.status = p->keep_status ? nullptr : ws_ptr<int>(p, p->off_status);
   k_init_tables<<<8, 256, 0, st>>>(a);
   int s = launch_status();
   if (s) return s;

@@ -12,7 +12,8 @@
 //             x[2p] + i x[2p+1], z-FFT, split into the two rows' half spectra
 //   k_ys<n1>  (x, W kz columns) per CTA: y-FFT in place in the spectra
 //   k_xs<n0>  W (y, kz) columns per CTA: x-FFT of every frame of the batch,
-//             |F|^2 summed in FP32 in registers, one FP64 RMW of sf
+//             |F|^2 summed in FP32 in registers, one FP64 RMW of sf every
+//             kPowerFlush frames and after the last
 #include "msf_mixed.cuh"
 
 namespace msf {
@@ -178,17 +179,21 @@ __global__ void __launch_bounds__(kSmoothThreads) k_xs(SmXArgs a) {
         for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = fmaf(r[k2].x, r[k2].x, fmaf(r[k2].y, r[k2].y, acc[j][k2]));
       }
     }
-  }
+    if (b == a.nframes - 1 || b % kPowerFlush == kPowerFlush - 1) {
 #pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int it = j * NT + threadIdx.x;
-    const int l = it % W, k1 = it / W;
-    if ((I2 % NT == 0 || it < I2) && l < weff) {
-      double* d = a.sf + (int64_t)k1 * a.F + f0 + l;
+      for (int j = 0; j < PER; ++j) {
+        const int it = j * NT + threadIdx.x;
+        const int l = it % W, k1 = it / W;
+        if ((I2 % NT == 0 || it < I2) && l < weff) {
+          double* d = a.sf + (int64_t)k1 * a.F + f0 + l;
 #pragma unroll
-      for (int k2 = 0; k2 < A; ++k2) {
-        double* dk = d + (int64_t)B * k2 * a.F;
-        *dk = *dk + (double)acc[j][k2];
+          for (int k2 = 0; k2 < A; ++k2) {
+            double* dk = d + (int64_t)B * k2 * a.F;
+            *dk = *dk + (double)acc[j][k2];
+          }
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = 0.f;
       }
     }
   }

@@ -40,6 +40,12 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-constexpr long long kWaitLimit = 1LL << 26;  // try_wait polls before giving up (seconds)
+// Bounded waits poll mbarrier.try_wait at most this many times before giving
+// up (a copy lands within a few polls; the limit is seconds of polling).  A
+// plan with MSF_PLAN_DIAG_STALL gives its plane kernel kDiagWaitLimit.  (A
+// limit read from the global timer instead measured more registers in the
+// x pass, which sits at its occupancy's register budget.)
+constexpr long long kWaitLimit = 1LL << 26;
+constexpr long long kDiagWaitLimit = 1LL << 14;
 
 }  // namespace msf

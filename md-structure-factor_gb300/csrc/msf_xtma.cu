@@ -7,8 +7,9 @@
 // by an mbarrier, so the copy of item s+1 (and s+2) runs while item s is
 // transformed.  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed
 // over the frames of the tile in FP32, one FP64 read-modify-write of sf per
-// tile.  Waits are bounded: on timeout the kernel latches MSF_E_TIMEOUT in
-// the plan status word and returns.
+// tile every kPowerFlush frames and after the last.  Waits are bounded: on
+// timeout the kernel latches MSF_E_TIMEOUT in the plan status word and
+// returns.
 #include "msf_ct.cuh"
 #include "msf_r2.cuh"
 #include "msf_tma.cuh"
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
       }
     }
     const int frame = s % a.nframes;
-    if (frame == a.nframes - 1) {
+    if (frame == a.nframes - 1 || frame % kPowerFlush == kPowerFlush - 1) {
       const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
       const int64_t f0 = (int64_t)tile * W;
 #pragma unroll

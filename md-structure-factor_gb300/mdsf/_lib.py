@@ -93,6 +93,8 @@ SIGNATURES = {
     "msf_batch_destroy": (c_int, [c_p]),
     "msf_hist_sf_f32_noalloc": (c_int, [c_p, c_i64, c_i64, c_p, c_int, c_int, c_int, c_int, c_p, c_p]),
     "msf_noalloc_scratch_bytes": (c_size, []),
+    "msf_noalloc_init": (c_int, [c_int, c_int, c_int, c_p, c_p]),
+    "msf_noalloc_status": (c_int, [c_p]),
     "msf_gro_scan": (c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "msf_gro_read": (c_int, [C.c_char_p, C.c_int64, C.c_int64, c_p, c_p, c_p, c_int]),
     "msf_trr_scan": (c_int, [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

@@ -18,6 +18,7 @@ import math
 import numpy as np
 import torch
 
+from . import tune as _tune
 from ._lib import MSF_WRAP, c_p, call
 from .plan import get_plan, stream_ptr
 
@@ -90,7 +91,7 @@ def _launch_chain(plan, code, p, w, N, T, sc, flags, sf, st):
 
 
 def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False, mean=False,
-                     out=None, device=None, tuning=None, stream_chunk=None, zero_copy=False):
+                     out=None, device=None, tuning=None, stream_chunk=None, zero_copy=False, scale=None):
     """Sum over frames of |rfftn(histogram)|^2, FP64, shape (n0, n1, n2//2+1).
 
     positions: (T, N, 3) or (N, 3) float32/float64, or (T, N, 4) float32 with
@@ -113,14 +114,28 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
       otherwise atoms outside [0, L] are dropped (numpy.histogramdd range).
     mean: divide by the frame count (the reference saves the undivided sum).
     out: FP64 tensor to accumulate into (not zeroed).
+    tuning: plan fields (variant, batch, tile_w, ...); None takes the
+      autotuner's cached tuning for this grid shape on this GPU (see
+      :mod:`mdsf.tune`), or the plan defaults when the cache has none.
+    scale: (T, 3) per-frame rescale factors given explicitly, with ``box``
+      the (3,) binning box: a slice of a longer trajectory then bins as the
+      whole trajectory does (factors and mean box of dens.py:50-53 computed
+      over every frame, see :func:`mdsf.shard.shard_inputs`).
     """
     device = _dev(device)
     pos = positions
     if pos.ndim == 2:
         pos = pos[None]
     T, N, C = pos.shape
-    scale, L = frame_scale(box)
-    kw = dict(tuning or {})
+    if scale is None:
+        scale, L = frame_scale(box)
+    else:
+        L = np.asarray(box.detach().cpu().numpy() if isinstance(box, torch.Tensor) else box, dtype=np.float64)
+        scale = np.asarray(scale.detach().cpu().numpy() if isinstance(scale, torch.Tensor) else scale,
+                           dtype=np.float64)
+        if L.shape != (3,) or scale.shape != (T, 3):
+            raise ValueError("with scale=, box must be the (3,) binning box and scale (T, 3)")
+    kw = dict(tuning) if tuning is not None else dict(_tune.lookup(grid_dims) or {})
     kw.setdefault("max_atoms", N)
     plan = get_plan(grid_dims, L, device=device, **kw)
     if out is None:

@@ -22,14 +22,32 @@ class BatchedSystems:
     """systems: list of dicts with keys
     ``pos_w`` (T, N, 4) float32 CUDA tensor (x, y, z, electrons), ``box`` (3,),
     ``dims`` (n0, n1, n2) and optionally ``wrap``, ``batch``, ``variant``, ``tile_w``.
-    The ``sf`` attribute holds one FP64 accumulator per system.
+    The ``sf`` attribute holds one FP64 accumulator per system.  A system
+    without ``batch``/``variant``/``tile_w`` takes the autotuner's cached
+    tuning of its grid shape (:mod:`mdsf.tune`); with ``autotune=True`` shapes
+    missing from the cache are tuned first (``tune_candidates`` candidates
+    each, at the system's atom count).
     """
 
-    def __init__(self, systems, n_streams=4, device=None):
+    def __init__(self, systems, n_streams=4, device=None, autotune=False, tune_candidates=4):
+        from . import tune as _tune
         self._lib = load()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.systems = list(systems)
         n = len(self.systems)
+        self.tuned_shapes = 0
+        tunings = []
+        for s in self.systems:
+            dims = tuple(int(v) for v in s["dims"])
+            if any(k in s for k in ("batch", "variant", "tile_w")):
+                tunings.append({})
+                continue
+            t = _tune.lookup(dims)
+            if t is None and autotune:
+                t = _tune.tune(dims, n_atoms=int(s["pos_w"].shape[1]), max_candidates=tune_candidates,
+                               frames=16, device=self.device)
+                self.tuned_shapes += 1
+            tunings.append(t or {})
         arr = (_lib.BatchSystem * n)()
         self.sf = []
         self._keep = []
@@ -49,9 +67,9 @@ class BatchedSystems:
             arr[i].box = (C.c_double * 3)(*[float(b) for b in s["box"]])
             arr[i].n0, arr[i].n1, arr[i].n2 = d0, d1, d2
             arr[i].flags = _lib.MSF_WRAP if s.get("wrap") else 0
-            arr[i].batch = int(s.get("batch", 0))
-            arr[i].variant = int(s.get("variant", 0))
-            arr[i].tile_w = int(s.get("tile_w", 0))
+            arr[i].batch = int(s.get("batch", tunings[i].get("batch", 0)))
+            arr[i].variant = int(s.get("variant", tunings[i].get("variant", 0)))
+            arr[i].tile_w = int(s.get("tile_w", tunings[i].get("tile_w", 0)))
         h = c_p()
         call("msf_batch_create", C.byref(h), arr, n, int(n_streams))
         self._h = h

@@ -29,6 +29,23 @@ def reduce_sf(sf, group=None):
     return sf
 
 
+def shard_inputs(n_frames, box, rank, world):
+    """(start, stop, scale, L) of `rank`'s frames.
+
+    With per-frame boxes (T, 3) the reference rescales every frame to the
+    mean box of the WHOLE trajectory and bins in that box (dens.py:50-58), so
+    the factors avg/box_t and the mean box are computed over all T frames
+    first and each rank takes its rows of the factors: every rank then builds
+    the same grid and bins exactly as one process would.  ``scale`` is None
+    for a single (3,) box."""
+    from .api import frame_scale
+    a, b = shard_range(n_frames, rank, world)
+    scale, L = frame_scale(box)
+    if scale is not None and scale.shape[0] != n_frames:
+        raise ValueError("per-frame boxes must have one row per frame")
+    return a, b, (None if scale is None else scale[a:b]), L
+
+
 def structure_factor_sharded(positions, box, weights, grid_dims, rank=None, world=None, **kw):
     """Each rank runs :func:`mdsf.structure_factor` on its frames, then one all-reduce."""
     from .api import structure_factor
@@ -36,7 +53,6 @@ def structure_factor_sharded(positions, box, weights, grid_dims, rank=None, worl
         rank = dist.get_rank() if dist.is_initialized() else 0
     if world is None:
         world = dist.get_world_size() if dist.is_initialized() else 1
-    a, b = shard_range(positions.shape[0], rank, world)
-    bx = box[a:b] if getattr(box, "ndim", 1) == 2 else box
-    sf = structure_factor(positions[a:b], bx, weights, grid_dims, **kw)
+    a, b, scale, L = shard_inputs(positions.shape[0], box, rank, world)
+    sf = structure_factor(positions[a:b], L, weights, grid_dims, scale=scale, **kw)
     return reduce_sf(sf)

@@ -10,6 +10,8 @@ so the workloads are generated from ``numpy.random.default_rng(seed)``:
   background, Gaussian thermal noise per frame.
 * :func:`uniform_system` -- uniform atoms with weights from {1, 6, 7, 8}.
 * :func:`smooth_sizes` -- the 2^a 3^b 5^c grid sizes in a range.
+* :func:`ewald_q_set` -- q vectors on the three Ewald-sphere slices of
+  plot2d.py:236-255 plus a |q| shell (the differentiable workload).
 
 Positions are wrapped into [0, L) (``np.mod``, then clamped below L in the
 output precision).
@@ -115,3 +117,40 @@ def pack_float4(pos, w):
     out[..., :3] = pos
     out[..., 3] = np.asarray(w, np.float32)
     return out
+
+
+def ewald_q_set(m=65_536, wavelength=0.154, extent=15.0, shell=(5.0, 15.0), seed=6):
+    """(m, 3) float32 q vectors (nm^-1): three Ewald-sphere slices and a shell.
+
+    Each slice is an n x n grid of in-plane points (a, b) in [-extent,
+    extent]^2 lifted onto the sphere of radius K = 2 pi / wavelength as
+    plot2d.py:236-255 does (theta = atan(sqrt(a^2 + b^2) / K), in-plane
+    coordinates times cos(theta), the third K (1 - cos(theta)); xy, xz, yz
+    planes), n = the largest power of two with 3 n^2 <= 3m/4; the rest are
+    uniform directions with |q| uniform in ``shell``."""
+    rng = np.random.default_rng(seed)
+    K = 2.0 * np.pi / wavelength
+    n = 1
+    while 3 * (2 * n) ** 2 <= 3 * m // 4:
+        n *= 2
+    ax = np.linspace(-extent, extent, n)
+    a, b = np.meshgrid(ax, ax, indexing="ij")
+    c = np.cos(np.arctan(np.sqrt(a * a + b * b) / K))
+    h = K * (1.0 - c)
+    slices = [np.stack([a * c, b * c, h], -1), np.stack([a * c, h, b * c], -1), np.stack([h, a * c, b * c], -1)]
+    q = [s.reshape(-1, 3) for s in slices]
+    rest = m - 3 * n * n
+    d = rng.standard_normal((rest, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    q.append(d * rng.uniform(shell[0], shell[1], (rest, 1)))
+    return np.concatenate(q).astype(np.float32)
+
+
+def direct_system(n_atoms=20_000, L=6.0, seed=0, sigma=0.05):
+    """(r (N,3) float32 in a cubic box, f (N,) float32 from {1,6,7,8},
+    r_target = r + N(0, sigma) float32): the differentiable workload."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(0.0, L, (n_atoms, 3)).astype(np.float32)
+    f = rng.choice(np.array([1, 6, 7, 8], np.float32), n_atoms)
+    rt = (r + rng.normal(0.0, sigma, r.shape)).astype(np.float32)
+    return r, f, rt

@@ -75,3 +75,43 @@ def fd_grad(r, f, q, target, h=1e-5, atoms=None):
             lm, _ = loss_log1p_mse(sf(rm, f, q), target)
             out[k, d] = (lp - lm) / (2 * h)
     return out
+
+
+def grad_chunk(r, f, q, g, A, B):
+    """The part of (dL/dr, dL/df) that the q vectors ``q`` (with their dL/dS
+    ``g`` and amplitudes A, B of the whole system) contribute: :func:`grad`
+    is the sum of these over any split of the q set."""
+    r = np.asarray(r, np.float64)
+    f = np.asarray(f, np.float64)
+    q = np.asarray(q, np.float64)
+    ph = q @ r.T
+    c, sn = np.cos(ph), np.sin(ph)
+    gb = (np.asarray(g, np.float64) * B)[:, None]
+    ga = (np.asarray(g, np.float64) * A)[:, None]
+    w = gb * c - ga * sn
+    return 2.0 * f[:, None] * (w.T @ q), 2.0 * ((ga * c + gb * sn).sum(0))
+
+
+def fd_grad_moved(r, f, q, target, A, B, h=1e-5, atoms=(0,)):
+    """Central finite differences of the log1p-MSE loss in FP64, one atom
+    coordinate at a time: moving atom j changes only its own term of the
+    amplitudes, so A, B of the unmoved system are updated by that term
+    instead of being summed again (the same FP64 loss, O(M) per point)."""
+    r = np.asarray(r, np.float64)
+    f = np.asarray(f, np.float64)
+    q = np.asarray(q, np.float64)
+    out = np.zeros((len(atoms), 3))
+    for k, j in enumerate(atoms):
+        ph0 = q @ r[j]
+        c0, s0 = np.cos(ph0), np.sin(ph0)
+        for d in range(3):
+            lv = []
+            for sgn in (1.0, -1.0):
+                rj = r[j].copy()
+                rj[d] += sgn * h
+                ph = q @ rj
+                Ap = A + f[j] * (np.cos(ph) - c0)
+                Bp = B + f[j] * (np.sin(ph) - s0)
+                lv.append(loss_log1p_mse(Ap * Ap + Bp * Bp, target)[0])
+            out[k, d] = (lv[0] - lv[1]) / (2 * h)
+    return out

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a container where the reference checkout is present:
+Run in a container where the reference checkout is present, giving its
+path (required):
 
-    python tests/golden/make_golden.py /root/reference [--radial | --rz]
+    python tests/golden/make_golden.py <reference dir> [--radial | --rz | --water]
 
 It imports the reference's ``dens.py`` and ``plot2d.py`` directly (their
 missing third-party modules -- ``past.utils``, ``tqdm`` progress bars and
@@ -25,6 +26,12 @@ Fixtures:
   rz_*.npz     -- ``measure_intensity.py`` run as a script: the inputs and
                   outputs of its two ``histogram2d`` calls, the plotted Hrz
                   and the line it writes (``--rz`` makes these alone).
+  gauss_water.npz -- ``dens.compute_sf`` on the 1,500-water box (4,500 O/H
+                  atoms, 25 Angstrom, 2 frames, Sres giving 64^3): the seed
+                  and the inputs, ``sf`` and ``sfplt`` stored as float32 (the
+                  parity bar is 1e-5 of max(S)), ``L``, ``N``, the in-place
+                  ``r`` and SHA-256 digests of the float64 ``kgrid`` and of
+                  the q channels of ``kgridplt`` (``--water`` makes it alone).
 """
 from __future__ import annotations
 
@@ -312,10 +319,56 @@ def main_rz(ref):
         os.chdir(cwd)
 
 
+def water_case(seed=1, frames=2):
+    """The water box of the plain-method workload (1,500 rigid waters, O-H
+    0.9572 A, 104.52 deg), in Angstrom for the reference: 25 A cube, types
+    O / H, Sres = 25/64 A, so the grid is 64^3."""
+    root = os.path.dirname(os.path.dirname(HERE))
+    sys.path.insert(0, os.path.join(root, "md-structure-factor_gb300"))
+    from mdsf import synth
+    pos, box, _ = synth.water_box(n_waters=1500, L=2.5, frames=frames, seed=seed)
+    r = pos * 10.0
+    L = np.tile(box * 10.0, (frames, 1))
+    typ = np.array(["O", "H", "H"] * 1500, dtype=object)
+    return dict(r=r, L=L, typ=typ, ucell=np.eye(3), Sres=25.0 / 64)
+
+
+def main_water(ref, seed=1, frames=2):
+    """dens.compute_sf run by the reference on the 4,500-atom water box."""
+    import hashlib
+    _install_stubs()
+    sys.path.insert(0, ref)
+    import dens
+    dens.tqdm.tqdm = _Quiet
+    rad = dens.load_radii(os.path.join(ref, "radii.txt"))
+    c = water_case(seed, frames)
+    r_in, L_in = c["r"].copy(), c["L"].copy()
+    out = os.path.join(tempfile.mkdtemp(), "water")
+    with contextlib.redirect_stdout(io.StringIO()):
+        dens.compute_sf(c["r"], c["L"], c["typ"], out, rad, c["ucell"], c["Sres"])
+    z = np.load(out + ".npz")
+
+    def digest(a):
+        return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()
+    np.savez_compressed(os.path.join(HERE, "gauss_water.npz"), seed=seed, frames=frames, Sres=c["Sres"],
+                        r=r_in, L_in=L_in, r_after=c["r"], rad_names=np.array(["H", "O"]),
+                        rad_nel=np.array([rad["H"][0], rad["O"][0]]),
+                        rad_sigma=np.array([rad["H"][1], rad["O"][1]]),
+                        out_sf32=z["sf"].astype(np.float32), out_sfplt32=z["sfplt"].astype(np.float32),
+                        out_sf_max=z["sf"].max(), out_L=z["L"], out_N=z["N"],
+                        kgrid_sha256=digest(z["kgrid"]), kgridplt_q_sha256=digest(z["kgridplt"][..., :3]),
+                        shapes=np.array([z["sf"].shape, z["sfplt"].shape]))
+    print("gauss_water", {k: z[k].shape for k in z.files})
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_dir = args[0] if args else "/root/reference"
-    if "--radial" in sys.argv:
+    if not args:
+        sys.exit("usage: make_golden.py <reference dir> [--radial | --rz | --water]")
+    ref_dir = args[0]
+    if "--water" in sys.argv:
+        main_water(ref_dir)
+    elif "--radial" in sys.argv:
         main_radial(ref_dir)
     elif "--rz" in sys.argv:
         main_rz(ref_dir)

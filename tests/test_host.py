@@ -9,6 +9,7 @@ import pytest
 from conftest import GOLDEN
 from mdsf import dens as mdens
 from mdsf import synth
+from mdsf import tune as _tune
 from mdsf.api import plot_axes
 
 GAUSS = ["gauss_ortho", "gauss_tcl", "gauss_corner"]
@@ -76,3 +77,9 @@ def test_generators_shapes_and_bounds():
     ok = np.abs(d - 0.09572) < 1e-9
     assert ok.mean() > 0.8            # molecules not cut by the wrap keep the bond length
     assert 48 in synth.smooth_sizes() and 243 in synth.smooth_sizes() and 49 not in synth.smooth_sizes()
+
+
+def test_candidates_cover_the_fused_and_generic_chains():
+    assert {c["variant"] for c in _tune.candidates((256, 256, 128))} == {3, 4}
+    assert {c["variant"] for c in _tune.candidates((75, 48, 81))} == {4}
+    assert {c["variant"] for c in _tune.candidates((74, 64, 26))} <= {1, 2}

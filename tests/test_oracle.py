@@ -53,6 +53,30 @@ def test_compute_sf_restatement_matches_reference(name):
     np.testing.assert_array_equal(out["kgridplt"][..., :3], z["out_kgridplt"][..., :3])
 
 
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()
+
+
+def test_compute_sf_restatement_water_box():
+    """The 4,500-atom water box at 64^3 (2 frames) run by the reference: sf
+    and sfplt stored in float32, so the bar is that rounding (6e-8 of each
+    value) instead of 1e-11."""
+    z = load("gauss_water")
+    rad = rad_of(z)
+    r = z["r"].copy()
+    out = odens.compute_sf(r, z["L_in"].copy(), np.array(["O", "H", "H"] * 1500, dtype=object), rad, np.eye(3),
+                           float(z["Sres"]))
+    np.testing.assert_array_equal(out["N"], z["out_N"])
+    np.testing.assert_array_equal(out["L"], z["out_L"])
+    np.testing.assert_array_equal(r, z["r_after"])
+    assert out["sf"].max() == z["out_sf_max"]
+    np.testing.assert_allclose(out["sf"], z["out_sf32"], rtol=1e-7, atol=1e-12 * float(z["out_sf_max"]))
+    np.testing.assert_allclose(out["sfplt"], z["out_sfplt32"], rtol=1e-7, atol=1e-12 * float(z["out_sf_max"]))
+    assert _sha(out["kgrid"]) == str(z["kgrid_sha256"])
+    assert _sha(out["kgridplt"][..., :3]) == str(z["kgridplt_q_sha256"])
+
+
 @pytest.mark.parametrize("name", GAUSS)
 def test_get_dplot_exact(name):
     z = load(name)

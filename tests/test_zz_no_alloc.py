@@ -28,14 +28,24 @@ def _ref_sf(p4, box, dims):
     return sf
 
 
+def _stream():
+    return c_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _noalloc_into(sf, p4, box, dims, flags=0):
+    lib = mdsf.load()
+    bx = (C.c_double * 3)(*box)
+    return lib.msf_hist_sf_f32_noalloc(c_p(p4.data_ptr()), p4.shape[1], p4.shape[0], C.cast(bx, c_p),
+                                       dims[0], dims[1], dims[2], flags, c_p(sf.data_ptr()), _stream())
+
+
 def _noalloc_sf(p4, box, dims):
     lib = mdsf.load()
     sf = torch.zeros((dims[0], dims[1], dims[2] // 2 + 1), dtype=torch.float64, device="cuda")
-    bx = (C.c_double * 3)(*box)
-    st = lib.msf_hist_sf_f32_noalloc(c_p(p4.data_ptr()), p4.shape[1], p4.shape[0], C.cast(bx, c_p),
-                                     dims[0], dims[1], dims[2], 0, c_p(sf.data_ptr()),
-                                     c_p(torch.cuda.current_stream().cuda_stream))
+    assert lib.msf_noalloc_init(dims[0], dims[1], dims[2], c_p(sf.data_ptr()), _stream()) == 0
+    st = _noalloc_into(sf, p4, box, dims)
     assert st == 0, lib.msf_strerror(st)
+    assert lib.msf_noalloc_status(_stream()) == 0
     return sf
 
 
@@ -52,6 +62,36 @@ def test_noalloc_matches_plan_entry_point_on_two_calls():
         torch.cuda.synchronize()
         err = float((got - ref).abs().max() / ref.abs().max())
         assert err < TOL, (dims, err)
+
+
+def test_noalloc_call_after_init_takes_no_device_memory():
+    """After msf_noalloc_init (and one call) on a grid, further calls leave
+    the device's free memory unchanged: nothing is allocated, not even by
+    loading."""
+    lib = mdsf.load()
+    dims, box = (64, 64, 64), (2.0, 2.0, 2.0)
+    pos, bx, w = synth.uniform_system(8000, box, frames=4, seed=23)
+    p4 = torch.from_numpy(synth.pack_float4(pos, w)).cuda()
+    sf = torch.zeros((64, 64, 33), dtype=torch.float64, device="cuda")
+    assert lib.msf_noalloc_init(64, 64, 64, c_p(sf.data_ptr()), _stream()) == 0
+    torch.cuda.synchronize()
+    assert float(sf.abs().max()) == 0.0          # the init's placeholder atom adds nothing
+    assert _noalloc_into(sf, p4, bx, dims) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for flags in (0, 1):                           # both binning modes were loaded by the init
+        assert _noalloc_into(sf, p4, bx, dims, flags) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert lib.msf_noalloc_status(_stream()) == 0
+
+
+def test_noalloc_refuses_continue():
+    lib = mdsf.load()
+    sf = torch.zeros((8, 8, 5), dtype=torch.float64, device="cuda")
+    p4 = torch.zeros((1, 10, 4), dtype=torch.float32, device="cuda")
+    assert _noalloc_into(sf, p4, (1.0, 1.0, 1.0), (8, 8, 8), flags=2) == -1   # MSF_CONTINUE: MSF_E_INVALID
+    assert lib.msf_noalloc_status(_stream()) == 0
 
 
 def test_noalloc_rejects_grids_beyond_the_scratch():
