@@ -222,3 +222,20 @@ def test_full_workload_properties():
     a = mdsf.structure_factor(p4[:batch], box, None, dims)
     b = mdsf.structure_factor(p4[batch:], box, None, dims)
     assert torch.equal(a + b, sf)
+
+
+def test_sharded_frames_sum_to_the_one_call_sf():
+    """structure_factor_sharded's two shards (rank 0 and 1 of 2, run one
+    after another without a process group) with per-frame boxes: every shard
+    bins in the trajectory's mean box, so their sum is the one-call sf."""
+    from mdsf.shard import structure_factor_sharded
+    rng = np.random.default_rng(12)
+    T, N = 7, 20_000
+    boxes = np.array([3.0, 2.6, 2.8]) * (1 + 0.02 * rng.standard_normal((T, 1)))
+    pos = (rng.uniform(0, 1, (T, N, 3)) * np.array([3.0, 2.6, 2.8])).astype(np.float32)
+    w = rng.integers(1, 9, N).astype(np.int32)
+    one = mdsf.structure_factor(pos, boxes, w, (64, 48, 56)).cpu().numpy()
+    parts = [structure_factor_sharded(pos, boxes, w, (64, 48, 56), rank=r, world=2).cpu().numpy() for r in (0, 1)]
+    assert rel_err(parts[0] + parts[1], one) < 1e-6
+    ref = ohist.hist_sf(pos, boxes, w, (64, 48, 56))
+    assert rel_err(parts[0] + parts[1], ref) < TOL
