@@ -8,8 +8,18 @@
 // as an unevaluated sum hi + lo (split from FP64), each product q_i r_i is
 // formed with its exact FMA residual, every component is reduced by its own
 // nearest integer (exact), and the small remainders are summed: the phase
-// error is then a few 1e-7 turn whatever |q.r| is.  Partial sums over one
-// shared-memory tile are FP32 and are added to FP64 running sums per tile.
+// error is then a few 1e-7 turn whatever |q.r| is.
+//
+// Summation: in the forward pass each thread sums its q's terms over groups
+// of kDGroup atoms in plain FP32, adds each group sum into the tile's FP32
+// partial with a compensated (Kahan) addition, and adds the tile partials
+// (kDTile atoms) into FP64 running sums.  A plain FP32 sum over the tile
+// leaves A and B with absolute errors near 1e-2 at 20k atoms, which the
+// log(1 + S) loss turns into gradient errors of ~4e-4 through the q vectors
+// of small S; the grouped compensated sum keeps them near 2e-4 (measured on
+// a numpy emulation: gradient error 2e-6 against FP64) for 0.5 extra FP32
+// operations per (atom, q) pair.  The adjoint's sums (no small-S
+// amplification) stay plain FP32 per tile.
 //
 // Forward: A_q = sum f cos, B_q = sum f sin, S_q = A^2 + B^2.
 // Adjoint (upstream g_q = dL/dS_q), recomputing the phases:
@@ -22,6 +32,7 @@ namespace msf {
 constexpr int kDThreads = 256;
 constexpr int kDPer = 2;                       // q (fwd) or atoms (bwd) per thread
 constexpr int kDTile = 512;                    // atoms (fwd) or q (bwd) per smem tile
+constexpr int kDGroup = 16;                    // atoms per plain FP32 group sum (fwd)
 constexpr float k2Pi = 6.28318530717958648f;
 
 // q in turns as hi + lo pairs: (hx, hy, hz) and (lx, ly, lz)
@@ -73,21 +84,43 @@ __global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restri
     __syncthreads();
     for (int i = threadIdx.x; i < na; i += kDThreads) tile[i] = __ldg(R + a0 + i);
     __syncthreads();
-    float pa[kDPer], pb[kDPer];
+    // tile partials with their Kahan compensations
+    float pa[kDPer], pb[kDPer], ca[kDPer], cb[kDPer];
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) { pa[k] = 0.f; pb[k] = 0.f; }
-    for (int i = 0; i < na; ++i) {
-      const float4 r = tile[i];
+    for (int k = 0; k < kDPer; ++k) { pa[k] = 0.f; pb[k] = 0.f; ca[k] = 0.f; cb[k] = 0.f; }
+    for (int i0 = 0; i0 < na; i0 += kDGroup) {
+      const int i1 = min(i0 + kDGroup, na);
+      float ga[kDPer], gb[kDPer];
+#pragma unroll
+      for (int k = 0; k < kDPer; ++k) { ga[k] = 0.f; gb[k] = 0.f; }
+      for (int i = i0; i < i1; ++i) {
+        const float4 r = tile[i];
+#pragma unroll
+        for (int k = 0; k < kDPer; ++k) {
+          float s, c;
+          phase_sincos(tq[k], r, &s, &c);
+          ga[k] = fmaf(r.w, c, ga[k]);
+          gb[k] = fmaf(r.w, s, gb[k]);
+        }
+      }
 #pragma unroll
       for (int k = 0; k < kDPer; ++k) {
-        float s, c;
-        phase_sincos(tq[k], r, &s, &c);
-        pa[k] = fmaf(r.w, c, pa[k]);
-        pb[k] = fmaf(r.w, s, pb[k]);
+        // compensated additions (round-to-nearest intrinsics: not contracted)
+        const float ya = __fsub_rn(ga[k], ca[k]);
+        const float ta = __fadd_rn(pa[k], ya);
+        ca[k] = __fsub_rn(__fsub_rn(ta, pa[k]), ya);
+        pa[k] = ta;
+        const float yb = __fsub_rn(gb[k], cb[k]);
+        const float tb = __fadd_rn(pb[k], yb);
+        cb[k] = __fsub_rn(__fsub_rn(tb, pb[k]), yb);
+        pb[k] = tb;
       }
     }
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) { A[k] += (double)pa[k]; B[k] += (double)pb[k]; }
+    for (int k = 0; k < kDPer; ++k) {
+      A[k] += (double)pa[k] - (double)ca[k];
+      B[k] += (double)pb[k] - (double)cb[k];
+    }
   }
 #pragma unroll
   for (int k = 0; k < kDPer; ++k) {

@@ -208,8 +208,8 @@ struct PlaneShape {
 //   edge line, k1 = 0 and B/2: two self-paired items in one unit.
 // That is B*n2/2 units of equal transform work: exactly two per thread at
 // the headline size, with no tail.  Edge units come first.
-template <int N1, int N2, int SP, int NT>
-__device__ __forceinline__ void ypass2_split(const float2* buf, float2* out) {
+template <int N1, int N2, int SP, int NT, bool ZERO = false>
+__device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   constexpr int P = N1 / 2, NH = N2 / 2 + 1;
   constexpr int A = r2::Split2<P>::A, B = r2::Split2<P>::B;
   constexpr int KM = N2 / 2 - 1;          // interior output lines 1 .. n2/2 - 1
@@ -235,11 +235,18 @@ __device__ __forceinline__ void ypass2_split(const float2* buf, float2* out) {
       lp = N2 - l;
       k1p = (B - k1) & (B - 1);
     }
-    const float2* pa = buf + l * SP + A * k1;
-    const float2* pb = buf + lp * SP + A * k1p;
+    float2* pa = buf + l * SP + A * k1;
+    float2* pb = buf + lp * SP + A * k1p;
     float2 a[A], b[A];
 #pragma unroll
     for (int n1 = 0; n1 < A; ++n1) { a[n1] = pa[n1]; b[n1] = pb[n1]; }
+    if (ZERO) {
+      // every slot of the plane is read by exactly one unit (item and
+      // partner of each unit are distinct and cover all B*N2 items once):
+      // clearing what was read leaves the plane zeroed for the next deposit
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) { pa[n1] = make_float2(0.f, 0.f); pb[n1] = make_float2(0.f, 0.f); }
+    }
     reg::reg_dft<A>(a);
     reg::reg_dft<A>(b);
     if (u < B && k1 == 0) {
@@ -263,15 +270,17 @@ __device__ __forceinline__ void ypass2_split(const float2* buf, float2* out) {
 
 // z FFT of the row pairs, then the half-length y FFT with the real split:
 // the deposited plane in buf becomes the half plane at out.
-template <int N1, int N2>
+template <int N1, int N2, bool ZERO = false>
 __device__ __forceinline__ void plane_transform(float2* buf, float2* out) {
   using S = PlaneShape<N1, N2>;
-  // z: lines = pairs p, samples stride SP; then pass 1 of the half y FFT
-  // (lines = kz, samples stride 1), and its pass 2 fused with the real split
-  r2::fft2_lines_fn<N2, S::P, S::SP, 1, S::NT>(buf, CTw<N2>());
+  // z: lines = pairs p, samples stride SP (the two inner barriers over the
+  // warps that share lines only); then pass 1 of the half y FFT (lines = kz,
+  // samples stride 1), and its pass 2 fused with the real split
+  r2::fft2_lines_grouped<N2, S::P, S::SP, 1, S::NT>(buf, CTw<N2>());
+  __syncthreads();
   r2::pass1_fn<S::P, N2, 1, S::SP, S::NT>(buf, CTw<S::P>());
   __syncthreads();
-  ypass2_split<N1, N2, S::SP, S::NT>(buf, out);
+  ypass2_split<N1, N2, S::SP, S::NT, ZERO>(buf, out);
 }
 
 // float offset of voxel y*n2 + z in the row-pair layout buf[z][p].(y & 1)
@@ -371,6 +380,12 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
   };
   int2 after = make_int2(0, 0);   // thread 0: range of the plane after the next
   int item = blockIdx.x;
+  // the plane starts zeroed; afterwards the split of each plane clears what
+  // it reads, so the next deposit finds it zeroed again
+  {
+    int4* z4 = reinterpret_cast<int4*>(buf);
+    for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
+  }
   if (tid == 0) {
     mbar_init(bar, 1);
     ctl[2] = 0;
@@ -388,13 +403,11 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
   uint32_t phase = 0;
   for (; item < items; item += G) {
     const int frame = item / a.n0, x = item - frame * a.n0;
-    int4* z4 = reinterpret_cast<int4*>(buf);
-    for (int i = tid; i < N2 * SP / 2; i += NT) z4[i] = make_int4(0, 0, 0, 0);
     long long spins = 0;
     while (!mbar_try_wait(bar, phase)) {
       if (++spins > a.wait_limit) { atomicExch(ctl + 2, 1); break; }
     }
-    __syncthreads();
+    __syncthreads();   // also: the previous plane's split has read and cleared the plane
     if (ctl[2]) {
       if (tid == 0) atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
       break;
@@ -421,8 +434,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
       ctl[1] = after.y;
       if (next + G < items) after = range(next + G);
     }
-    plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
-    __syncthreads();   // the split has read buf before it is zeroed again
+    plane_transform<N1, N2, true>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
   }
   // leave no copy in flight into this CTA's shared memory (bounded)
   if (tid == 0 && ctl[2]) {

@@ -95,5 +95,56 @@ __device__ __forceinline__ void fft2_lines(float2* s, const float2* tw) {
   fft2_lines_fn<N, NL, SM, SL, NT>(s, [tw](int k) { return tw[k]; });
 }
 
+// Barrier over the threads that share lines with this one.  In pass1_fn and
+// fft2_lines_fn every item of thread t lies on line t % NL when NT is a
+// multiple of NL, so with NL a multiple of 32 the warps split into NL/32
+// groups that never touch each other's lines: a named barrier per group
+// (ids 1..8; 0 is __syncthreads) orders the passes of one group without
+// waiting for the others.  Otherwise a whole-block barrier.
+template <int NL, int NT>
+__device__ __forceinline__ void line_group_sync() {
+  if constexpr (NL % 32 == 0 && NT % NL == 0 && NL / 32 > 1 && NL / 32 <= 8) {
+    constexpr int G = NL / 32;
+    const int g = (int)(threadIdx.x % NL) / 32;
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(NT / G) : "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
+// fft2_lines_fn with its two inner barriers over line groups only; the
+// caller orders the result with a whole-block barrier before another
+// thread's lines are read.
+template <int N, int NL, int SM, int SL, int NT, typename TW>
+__device__ __forceinline__ void fft2_lines_grouped(float2* s, TW tw) {
+  constexpr int A = Split2<N>::A, B = Split2<N>::B;
+  pass1_fn<N, NL, SM, SL, NT>(s, tw);
+  line_group_sync<NL, NT>();
+  constexpr int ITEMS = B * NL;
+  constexpr int PER = (ITEMS + NT - 1) / NT;
+  float2 r[PER][A];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int it = j * NT + threadIdx.x;
+    if (ITEMS % NT == 0 || it < ITEMS) {
+      const int l = it % NL, k1 = it / NL;
+      const float2* p = s + l * SL + (A * k1) * SM;
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) r[j][n1] = p[n1 * SM];
+      reg::reg_dft<A>(r[j]);
+    }
+  }
+  line_group_sync<NL, NT>();
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int it = j * NT + threadIdx.x;
+    if (ITEMS % NT == 0 || it < ITEMS) {
+      const int l = it % NL, k1 = it / NL;
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) s[l * SL + (k1 + B * k2) * SM] = r[j][k2];
+    }
+  }
+}
+
 }  // namespace r2
 }  // namespace msf

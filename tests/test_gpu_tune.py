@@ -22,7 +22,7 @@ def test_tune_caches_and_is_used(tmp_path, monkeypatch):
     assert best is not None and best["variant"] in (3, 4)
     data = json.loads(cache.read_text())
     e = data[tune.key(dims)]
-    assert e["tried"] == 4 and e["tuning"] == best
+    assert 1 <= e["tried"] <= 4 and e["tuning"] == best     # tunings a plan refuses are skipped
     assert min(r["ms_per_frame"] for r in e["results"]) == e["ms_per_frame"]
     assert tune.lookup(dims) == best
     assert tune.tune_for(dims) == best                 # cached: no second tuning
