@@ -54,16 +54,16 @@ WAVELENGTH = 0.154
 METRIC = "frames/s at 256^2x128 grid, 200k atoms (batched, graph-captured hist->FFT->|F|^2->FP64 sum)"
 WORKLOAD = ("columnar 200k atoms, 16.0x13.856x8.0 nm, 256x256x128 grid, 100 frames/step, f32 positions, "
             "get_dplot + Ewald lambda=0.154 nm")
-# source-level operation counts of one (atom, q) pair of the direct sum
+# source-level FP32 operation counts of one (atom, q) pair of the direct sum
 # (msf_direct.cu): the phase in turns from hi + lo parts of q/2pi with FMA
-# residuals (3 x [FMUL, 2 FFMA, FRND, 2 FADD], 2 FADD, FRND + FADD, FMUL),
-# then __sincosf (2 MUFU) and the accumulation (2 FFMA forward; the adjoint's
+# residuals (3 x [FMUL, 2 FFMA, FRND, 2 FADD], 2 FADD, FRND + FADD), the
+# turn-based sin/cos (FMUL, FRND, FFMA, FMUL, 4 + 4 polynomial FMA/FMUL,
+# F2I, LOP, 2 selects, 2 sign selects: 17), then the accumulation (forward:
+# 2 FFMA and the grouped compensated sum, ~0.5 per pair; adjoint: the
 # weight, 3 gradient and 2 weight-gradient FMAs: 7)
-DIRECT_FP32_OPS = {"fwd": 25, "bwd": 30}
-DIRECT_MUFU_OPS = 2
+DIRECT_FP32_OPS = {"fwd": 41.5, "bwd": 46}
 SM_COUNT_FALLBACK = 152
 FP32_LANES_PER_SM = 128
-MUFU_LANES_PER_SM = 16
 
 
 def config(world):
@@ -809,14 +809,12 @@ def direct_extra(torch, dev, keep=None):
     for name, ms in (("fwd", fwd_ms / reps), ("bwd", bwd_ms / reps)):
         rate = pairs / (ms / 1000.0)
         fp32_ceiling = sms * FP32_LANES_PER_SM * mhz * 1e6 / DIRECT_FP32_OPS[name]
-        mufu_ceiling = sms * MUFU_LANES_PER_SM * mhz * 1e6 / DIRECT_MUFU_OPS
         res[f"direct_{name}_pairs_per_s"] = rate
         res[f"direct_{name}_frac_fp32_issue"] = rate / fp32_ceiling
-        res[f"direct_{name}_frac_mufu"] = rate / mufu_ceiling
     res["direct_roofline_note"] = (
-        f"ceilings at {mhz:.0f} MHz x {sms} SMs: FP32 issue = 128 lanes/SM / ops per pair "
-        f"({DIRECT_FP32_OPS['fwd']} forward, {DIRECT_FP32_OPS['bwd']} adjoint, source-level count incl. 4 FRND), "
-        f"MUFU = 16 lanes/SM / 2 (sin, cos); the binding one is FP32 issue")
+        f"ceiling at {mhz:.0f} MHz x {sms} SMs: FP32 issue = 128 lanes/SM / FP32 ops per pair "
+        f"({DIRECT_FP32_OPS['fwd']} forward, {DIRECT_FP32_OPS['bwd']} adjoint, source-level count; sin/cos are "
+        f"polynomials in turns on the FP32 pipe, no SFU)")
     if keep is not None:
         keep["_direct_S"] = (rs[0], fs[0], q_np, S[0].detach().cpu().numpy().astype(np.float64))
     del r, f, q, rr, S, g, target

@@ -3,23 +3,25 @@
 // power the reference computes at dens.py:313-316).
 //
 // Phases are computed in turns, t = (q/2pi).r, and reduced to [-1/2, 1/2]
-// before the SFU sin/cos (__sincosf(2 pi t) on [-pi, pi]).  With |q.r| up
-// to ~25 turns a plain FP32 product loses ~1e-5 rad, so each q/2pi is held
-// as an unevaluated sum hi + lo (split from FP64), each product q_i r_i is
-// formed with its exact FMA residual, every component is reduced by its own
-// nearest integer (exact), and the small remainders are summed: the phase
-// error is then a few 1e-7 turn whatever |q.r| is.
+// before sin/cos (sincos_turns: polynomials in turns, no 2 pi scaling).
+// With |q.r| up to ~25 turns a plain FP32 product loses ~1e-5 rad, so each
+// q/2pi is held as an unevaluated sum hi + lo (split from FP64), each
+// product q_i r_i is formed with its exact FMA residual, every component is
+// reduced by its own nearest integer (exact), and the small remainders are
+// summed: the phase error is then ~2e-8 turn (rms) whatever |q.r| is.
 //
-// Summation: in the forward pass each thread sums its q's terms over groups
-// of kDGroup atoms in plain FP32, adds each group sum into the tile's FP32
-// partial with a compensated (Kahan) addition, and adds the tile partials
-// (kDTile atoms) into FP64 running sums.  A plain FP32 sum over the tile
-// leaves A and B with absolute errors near 1e-2 at 20k atoms, which the
-// log(1 + S) loss turns into gradient errors of ~4e-4 through the q vectors
-// of small S; the grouped compensated sum keeps them near 2e-4 (measured on
-// a numpy emulation: gradient error 2e-6 against FP64) for 0.5 extra FP32
-// operations per (atom, q) pair.  The adjoint's sums (no small-S
-// amplification) stay plain FP32 per tile.
+// Accuracy that the log(1 + S) loss needs: its gradient is dominated by the
+// q vectors of small S, whose relative error is the absolute error of the
+// amplitudes A, B over |F|.  Errors that add coherently over the atoms
+// (a bias of the phase scale, a biased sin/cos) or a long FP32 running sum
+// move A and B by ~1e-3 at 20k atoms and the gradient by ~4e-4.  Hence the
+// unbiased turn-based sin/cos, and in the forward pass: each thread sums its
+// q's terms over groups of kDGroup atoms in plain FP32, adds each group sum
+// into the tile's FP32 partial with a compensated (Kahan) addition, and adds
+// the tile partials (kDTile atoms) into FP64 running sums.  A numpy
+// emulation of this arithmetic gives a gradient error of 5e-5 against FP64
+// at 20k atoms (the floor is the FP32 phase rounding).  The adjoint's sums
+// (no small-S amplification) stay plain FP32 per tile.
 //
 // Forward: A_q = sum f cos, B_q = sum f sin, S_q = A^2 + B^2.
 // Adjoint (upstream g_q = dL/dS_q), recomputing the phases:
@@ -33,7 +35,6 @@ constexpr int kDThreads = 256;
 constexpr int kDPer = 2;                       // q (fwd) or atoms (bwd) per thread
 constexpr int kDTile = 512;                    // atoms (fwd) or q (bwd) per smem tile
 constexpr int kDGroup = 16;                    // atoms per plain FP32 group sum (fwd)
-constexpr float k2Pi = 6.28318530717958648f;
 
 // q in turns as hi + lo pairs: (hx, hy, hz) and (lx, ly, lz)
 struct QTurns { float hx, hy, hz, lx, ly, lz; };
@@ -56,10 +57,37 @@ __device__ __forceinline__ float turn_frac(float hi, float lo, float r) {
   return (p - rintf(p)) + e;
 }
 
+// sin and cos of 2 pi t for t in [-1/2, 1/2] turns, without a rounded 2 pi
+// scaling the phase: the quadrant k = rint(4t) is taken off exactly
+// (r = t - k/4 in [-1/8, 1/8]), sin(2 pi r) and cos(2 pi r) are polynomials
+// in r^2 fitted for this build (near-minimax on [0, 1/8] by iteratively
+// reweighted least squares in FP64: errors 2.4e-9 and 4.7e-11 before FP32
+// rounding), and the quadrant rotates them.  Errors of the rounded
+// coefficients are odd (sin) or even (cos) functions of r whose means cancel
+// between opposite quadrants.  The SFU form __sincosf(2 pi t) instead
+// multiplies t by float(2 pi) and its own scale: a phase bias near 1e-8 of
+// the same sign for every atom, whose errors add coherently in
+// A = sum f cos, B = sum f sin (~1e-3 at 20k atoms); through the q of small S
+// the log(1 + S) loss's gradient then moved by ~4e-4.
+__device__ __forceinline__ void sincos_turns(float t, float* s, float* c) {
+  const float k = rintf(4.0f * t);
+  const float r = fmaf(-0.25f, k, t);
+  const float z = r * r;
+  const float ps = r * fmaf(fmaf(fmaf(-75.40099585508018f, z, 81.5925250459675f), z, -41.34166242174424f), z,
+                            6.283185287502589f);
+  const float pc = fmaf(fmaf(fmaf(fmaf(59.22042251089335f, z, -85.44285258833072f), z, 64.9393162129225f), z,
+                             -19.73920865037173f), z, 0.9999999999526074f);
+  const int q = (int)k & 3;
+  const float sv = (q & 1) ? pc : ps;
+  const float cv = (q & 1) ? ps : pc;
+  *s = (q >= 2) ? -sv : sv;                 // quadrants 2, 3
+  *c = (q == 1 || q == 2) ? -cv : cv;       // quadrants 1, 2
+}
+
 __device__ __forceinline__ void phase_sincos(const QTurns& q, float4 r, float* s, float* c) {
   float t = turn_frac(q.hx, q.lx, r.x) + turn_frac(q.hy, q.ly, r.y) + turn_frac(q.hz, q.lz, r.z);
   t -= rintf(t);
-  __sincosf(k2Pi * t, s, c);
+  sincos_turns(t, s, c);
 }
 
 __global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
