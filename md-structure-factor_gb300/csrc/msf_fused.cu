@@ -188,7 +188,17 @@ struct CTw {
 template <int N1, int N2>
 struct PlaneShape {
   static constexpr int P = N1 / 2;
-  static constexpr int SP = P + 1;      // odd line stride: conflict-free columns
+  // PAIRS: the z and y passes move two complex values per 16-byte access
+  // (where the z lines' second-pass radix is at most 8: two 16-point
+  // transforms of the longer z lines do not fit the register budget), with
+  // an even line stride of SP*8 = 16 (mod 128) bytes (P a multiple of 16) so
+  // that those accesses are free of bank conflicts along and across lines;
+  // otherwise 8-byte accesses and an odd line stride.  The shapes whose pair
+  // passes spill registers at the bucket kernel's register cap keep 8-byte
+  // accesses.
+  static constexpr bool PAIRS = r2::Split2<N2>::A <= 8 &&
+                                !((N1 == 64 && N2 == 128) || (N1 == 128 && N2 == 64) || (N1 == 256 && N2 <= 64));
+  static constexpr int SP = PAIRS ? P + 2 : P + 1;
   static constexpr int NH = N2 / 2 + 1;
   static constexpr int NT = (N2 * P >= 4096) ? 512 : 256;
   // plane, then the segment tables of the bucket gather
@@ -208,7 +218,7 @@ struct PlaneShape {
 //   edge line, k1 = 0 and B/2: two self-paired items in one unit.
 // That is B*n2/2 units of equal transform work: exactly two per thread at
 // the headline size, with no tail.  Edge units come first.
-template <int N1, int N2, int SP, int NT, bool ZERO = false>
+template <int N1, int N2, int SP, int NT, bool ZERO = false, bool PAIRS = false>
 __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   constexpr int P = N1 / 2, NH = N2 / 2 + 1;
   constexpr int A = r2::Split2<P>::A, B = r2::Split2<P>::B;
@@ -238,14 +248,28 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
     float2* pa = buf + l * SP + A * k1;
     float2* pb = buf + lp * SP + A * k1p;
     float2 a[A], b[A];
+    const float2 z = make_float2(0.f, 0.f);
+    if constexpr (PAIRS) {
 #pragma unroll
-    for (int n1 = 0; n1 < A; ++n1) { a[n1] = pa[n1]; b[n1] = pb[n1]; }
+      for (int n1 = 0; n1 < A; n1 += 2) {
+        r2::ld2(pa + n1, a[n1], a[n1 + 1]);
+        r2::ld2(pb + n1, b[n1], b[n1 + 1]);
+      }
+    } else {
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) { a[n1] = pa[n1]; b[n1] = pb[n1]; }
+    }
     if (ZERO) {
       // every slot of the plane is read by exactly one unit (item and
       // partner of each unit are distinct and cover all B*N2 items once):
       // clearing what was read leaves the plane zeroed for the next deposit
+      if constexpr (PAIRS) {
 #pragma unroll
-      for (int n1 = 0; n1 < A; ++n1) { pa[n1] = make_float2(0.f, 0.f); pb[n1] = make_float2(0.f, 0.f); }
+        for (int n1 = 0; n1 < A; n1 += 2) { r2::st2(pa + n1, z, z); r2::st2(pb + n1, z, z); }
+      } else {
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) { pa[n1] = z; pb[n1] = z; }
+      }
     }
     reg::reg_dft<A>(a);
     reg::reg_dft<A>(b);
@@ -273,14 +297,21 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
 template <int N1, int N2, bool ZERO = false>
 __device__ __forceinline__ void plane_transform(float2* buf, float2* out) {
   using S = PlaneShape<N1, N2>;
-  // z: lines = pairs p, samples stride SP (the two inner barriers over the
-  // warps that share lines only); then pass 1 of the half y FFT (lines = kz,
-  // samples stride 1), and its pass 2 fused with the real split
-  r2::fft2_lines_grouped<N2, S::P, S::SP, 1, S::NT>(buf, CTw<N2>());
+  // z: lines = pairs p, samples stride SP, two adjacent lines per 16-byte
+  // access (the two inner barriers over the warps that share lines only);
+  // then pass 1 of the half y FFT (lines = kz, samples stride 1, two adjacent
+  // samples per access), and its pass 2 fused with the real split
+  if constexpr (S::PAIRS) {
+    r2::fft2_linepairs<N2, S::P, S::SP, S::NT>(buf, CTw<N2>());
+    __syncthreads();
+    r2::pass1_samplepairs<S::P, N2, S::SP, S::NT>(buf, CTw<S::P>());
+  } else {
+    r2::fft2_lines_grouped<N2, S::P, S::SP, 1, S::NT>(buf, CTw<N2>());
+    __syncthreads();
+    r2::pass1_fn<S::P, N2, 1, S::SP, S::NT>(buf, CTw<S::P>());
+  }
   __syncthreads();
-  r2::pass1_fn<S::P, N2, 1, S::SP, S::NT>(buf, CTw<S::P>());
-  __syncthreads();
-  ypass2_split<N1, N2, S::SP, S::NT, ZERO>(buf, out);
+  ypass2_split<N1, N2, S::SP, S::NT, ZERO, S::PAIRS>(buf, out);
 }
 
 // float offset of voxel y*n2 + z in the row-pair layout buf[z][p].(y & 1)
@@ -331,7 +362,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
 // returns.  With a.stall (the plan's diagnostic option) the
 // first wait expects 16 bytes that no copy delivers, so it runs out: the
 // error path can be tested without any fault.
-constexpr int kPlanePrefetch = 2;
+constexpr int kPlanePrefetch = 4;
 
 template <int N1, int N2>
 struct BucketPlaneShape {

@@ -146,5 +146,112 @@ __device__ __forceinline__ void fft2_lines_grouped(float2* s, TW tw) {
   }
 }
 
+// ------------------------------------------------ two values per access
+// The plane kernel's passes with 16-byte shared-memory accesses: a thread
+// moves two complex values per load or store -- the same sample of two
+// adjacent lines (fft2_linepairs) or two adjacent samples of one line
+// (pass1_samplepairs) -- so each pass issues half the shared-memory
+// instructions.  Layout requirement: even line stride (16-byte alignment);
+// with a line stride of S complex values and S*8 = 16 (mod 128) bytes, eight
+// consecutive lanes cover eight different 16-byte bank groups in both
+// directions, so neither pass has bank conflicts.
+__device__ __forceinline__ void ld2(const float2* p, float2& a, float2& b) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  a = make_float2(t.x, t.y);
+  b = make_float2(t.z, t.w);
+}
+__device__ __forceinline__ void st2(float2* p, float2 a, float2 b) {
+  *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+
+// Full transform of NL lines (line l at s + l, unit line stride; sample n at
+// n*SM), natural order in and out; thread items cover the line pairs
+// (2lp, 2lp + 1).  The two inner barriers are over the warps that share line
+// pairs (line_group_sync over NL/2 pairs); the caller orders the result with
+// a whole-block barrier before other lines are read.
+template <int N, int NL, int SM, int NT, typename TW>
+__device__ __forceinline__ void fft2_linepairs(float2* s, TW tw) {
+  static_assert(NL % 2 == 0 && SM % 2 == 0, "pairs of lines, 16-byte aligned");
+  constexpr int A = Split2<N>::A, B = Split2<N>::B, NP = NL / 2;
+  constexpr int ITEMS1 = A * NP;
+#pragma unroll 1
+  for (int base_it = 0; base_it < ITEMS1; base_it += NT) {
+    const int it = base_it + threadIdx.x;
+    if (ITEMS1 % NT == 0 || it < ITEMS1) {
+      const int lp = it % NP, n1 = it / NP;
+      float2* p = s + 2 * lp + n1 * SM;
+      float2 u[B], v[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) ld2(p + n2 * A * SM, u[n2], v[n2]);
+      reg::reg_dft<B>(u);
+      reg::reg_dft<B>(v);
+#pragma unroll
+      for (int k1 = 1; k1 < B; ++k1) {
+        const float2 w = tw(n1 * k1);
+        u[k1] = cmul(u[k1], w);
+        v[k1] = cmul(v[k1], w);
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < B; ++k1) st2(p + k1 * A * SM, u[k1], v[k1]);
+    }
+  }
+  line_group_sync<NP, NT>();
+  constexpr int ITEMS2 = B * NP;
+  constexpr int PER = (ITEMS2 + NT - 1) / NT;
+  float2 r[PER][A], q[PER][A];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int it = j * NT + threadIdx.x;
+    if (ITEMS2 % NT == 0 || it < ITEMS2) {
+      const int lp = it % NP, k1 = it / NP;
+      const float2* p = s + 2 * lp + (A * k1) * SM;
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) ld2(p + n1 * SM, r[j][n1], q[j][n1]);
+      reg::reg_dft<A>(r[j]);
+      reg::reg_dft<A>(q[j]);
+    }
+  }
+  line_group_sync<NP, NT>();
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int it = j * NT + threadIdx.x;
+    if (ITEMS2 % NT == 0 || it < ITEMS2) {
+      const int lp = it % NP, k1 = it / NP;
+#pragma unroll
+      for (int k2 = 0; k2 < A; ++k2) st2(s + 2 * lp + (k1 + B * k2) * SM, r[j][k2], q[j][k2]);
+    }
+  }
+}
+
+// pass1_fn over NL lines (line l at s + l*SL, unit sample stride) with the
+// items (n1, l) and (n1 + 1, l) of one thread sharing their 16-byte loads.
+template <int N, int NL, int SL, int NT, typename TW>
+__device__ __forceinline__ void pass1_samplepairs(float2* s, TW tw) {
+  static_assert(SL % 2 == 0, "16-byte aligned lines");
+  constexpr int A = Split2<N>::A, B = Split2<N>::B;
+  static_assert(A % 2 == 0, "pairs of first-pass items");
+  constexpr int ITEMS = (A / 2) * NL;
+#pragma unroll 1
+  for (int base_it = 0; base_it < ITEMS; base_it += NT) {
+    const int it = base_it + threadIdx.x;
+    if (ITEMS % NT == 0 || it < ITEMS) {
+      const int l = it % NL, n1 = 2 * (it / NL);
+      float2* p = s + l * SL + n1;
+      float2 u[B], v[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) ld2(p + n2 * A, u[n2], v[n2]);
+      reg::reg_dft<B>(u);
+      reg::reg_dft<B>(v);
+#pragma unroll
+      for (int k1 = 1; k1 < B; ++k1) {
+        u[k1] = cmul(u[k1], tw(n1 * k1));
+        v[k1] = cmul(v[k1], tw((n1 + 1) * k1));
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < B; ++k1) st2(p + k1 * A, u[k1], v[k1]);
+    }
+  }
+}
+
 }  // namespace r2
 }  // namespace msf
