@@ -362,7 +362,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
 // returns.  With a.stall (the plan's diagnostic option) the
 // first wait expects 16 bytes that no copy delivers, so it runs out: the
 // error path can be tested without any fault.
-constexpr int kPlanePrefetch = 4;
+constexpr int kPlanePrefetch = 2;
 
 template <int N1, int N2>
 struct BucketPlaneShape {
