@@ -393,12 +393,16 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
   int* ctl = reinterpret_cast<int*>(bar + 1);   // [0] range begin, [1] count, [2] abort flag
   const int tid = threadIdx.x;
   const int G = gridDim.x;
-  // thread 0: range (begin, count) of plane `item`, and the copy of its
-  // first CAP entries
-  auto range = [&](int item) {
+  // thread 0: offsets (begin, end) of plane `item` in the compacted entries,
+  // and the copy of its first CAP entries.  The offsets of the plane after
+  // next are loaded one plane ahead and first used a plane later: a count
+  // formed right after the load stalled thread 0 -- and with it warp 0 and
+  // every barrier after it -- for ~3k cycles per plane (measured with clock64
+  // stamps), the latency of a global load under the kernel's own traffic.
+  auto range_raw = [&](int item) {
     const int frame = item / a.n0, x = item - frame * a.n0;
     const int* po = a.poff + (int64_t)frame * (a.n0 + 1) + x;
-    return make_int2(po[0], po[1] - po[0]);
+    return make_int2(po[0], po[1]);
   };
   auto issue = [&](int item, int2 r) {
     if (a.stall) {
@@ -409,7 +413,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     mbar_expect_tx(bar, (uint32_t)ns * sizeof(int2));
     if (ns > 0) bulk_load(staged, a.pbucket + (int64_t)(item / a.n0) * a.pstride + r.x, ns * sizeof(int2), bar);
   };
-  int2 after = make_int2(0, 0);   // thread 0: range of the plane after the next
+  int2 after = make_int2(0, 0);   // thread 0: offsets of the plane after the next
   int item = blockIdx.x;
   // the plane starts zeroed; afterwards the split of each plane clears what
   // it reads, so the next deposit finds it zeroed again
@@ -423,12 +427,13 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     int2 r = make_int2(0, 0);
     if (item < items) {
-      r = range(item);
+      r = range_raw(item);
+      r.y -= r.x;
       issue(item, r);
     }
     ctl[0] = r.x;
     ctl[1] = r.y;
-    if (item + G < items) after = range(item + G);
+    if (item + G < items) after = range_raw(item + G);
   }
   __syncthreads();
   uint32_t phase = 0;
@@ -457,13 +462,14 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     __syncthreads();   // staging area and the range consumed
     if (tid == 0) {
       const int next = item + G;
+      const int2 r = make_int2(after.x, after.y - after.x);   // loaded a plane ago
       if (next < items) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(next, after);
+        issue(next, r);
       }
-      ctl[0] = after.x;
-      ctl[1] = after.y;
-      if (next + G < items) after = range(next + G);
+      ctl[0] = r.x;
+      ctl[1] = r.y;
+      if (next + G < items) after = range_raw(next + G);
     }
     plane_transform<N1, N2, true>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
   }
