@@ -32,7 +32,8 @@
 namespace msf {
 
 constexpr int kDThreads = 256;
-constexpr int kDPer = 2;                       // q (fwd) or atoms (bwd) per thread
+constexpr int kDPerF = 4;                      // q per thread (forward)
+constexpr int kDPerB = 2;                      // atoms per thread (adjoint: 4 spill at its register budget)
 constexpr int kDTile = 512;                    // atoms (fwd) or q (bwd) per smem tile
 constexpr int kDGroup = 16;                    // atoms per plain FP32 group sum (fwd)
 
@@ -70,6 +71,9 @@ __device__ __forceinline__ float turn_frac(float hi, float lo, float r) {
 // A = sum f cos, B = sum f sin (~1e-3 at 20k atoms); through the q of small S
 // the log(1 + S) loss's gradient then moved by ~4e-4.
 __device__ __forceinline__ void sincos_turns(float t, float* s, float* c) {
+  // t in [-3/2, 3/2]: the quadrant k = rint(4t) (|k| <= 6) also takes off
+  // the whole turns, and t - k/4 is exact (Sterbenz: t and k/4 are within a
+  // factor 2 of each other for k != 0); only k mod 4 matters below
   const float k = rintf(4.0f * t);
   const float r = fmaf(-0.25f, k, t);
   const float z = r * r;
@@ -85,24 +89,23 @@ __device__ __forceinline__ void sincos_turns(float t, float* s, float* c) {
 }
 
 __device__ __forceinline__ void phase_sincos(const QTurns& q, float4 r, float* s, float* c) {
-  float t = turn_frac(q.hx, q.lx, r.x) + turn_frac(q.hy, q.ly, r.y) + turn_frac(q.hz, q.lz, r.z);
-  t -= rintf(t);
+  const float t = turn_frac(q.hx, q.lx, r.x) + turn_frac(q.hy, q.ly, r.y) + turn_frac(q.hz, q.lz, r.z);
   sincos_turns(t, s, c);
 }
 
-__global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
+__global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
                                                           const float4* __restrict__ q, int64_t n_q,
                                                           int64_t q_sys_stride, float* S, float2* AB) {
   __shared__ float4 tile[kDTile];
   const int sys = blockIdx.y;
   const float4* R = rf + sys * n_atoms;
   const float4* Q = q + sys * q_sys_stride;
-  QTurns tq[kDPer];
-  int64_t qi[kDPer];
-  double A[kDPer], B[kDPer];
+  QTurns tq[kDPerF];
+  int64_t qi[kDPerF];
+  double A[kDPerF], B[kDPerF];
 #pragma unroll
-  for (int k = 0; k < kDPer; ++k) {
-    qi[k] = (int64_t)blockIdx.x * kDThreads * kDPer + k * kDThreads + threadIdx.x;
+  for (int k = 0; k < kDPerF; ++k) {
+    qi[k] = (int64_t)blockIdx.x * kDThreads * kDPerF + k * kDThreads + threadIdx.x;
     float4 v = qi[k] < n_q ? __ldg(Q + qi[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
     tq[k] = q_turns(v);
     A[k] = 0.0; B[k] = 0.0;
@@ -113,18 +116,18 @@ __global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restri
     for (int i = threadIdx.x; i < na; i += kDThreads) tile[i] = __ldg(R + a0 + i);
     __syncthreads();
     // tile partials with their Kahan compensations
-    float pa[kDPer], pb[kDPer], ca[kDPer], cb[kDPer];
+    float pa[kDPerF], pb[kDPerF], ca[kDPerF], cb[kDPerF];
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) { pa[k] = 0.f; pb[k] = 0.f; ca[k] = 0.f; cb[k] = 0.f; }
+    for (int k = 0; k < kDPerF; ++k) { pa[k] = 0.f; pb[k] = 0.f; ca[k] = 0.f; cb[k] = 0.f; }
     for (int i0 = 0; i0 < na; i0 += kDGroup) {
       const int i1 = min(i0 + kDGroup, na);
-      float ga[kDPer], gb[kDPer];
+      float ga[kDPerF], gb[kDPerF];
 #pragma unroll
-      for (int k = 0; k < kDPer; ++k) { ga[k] = 0.f; gb[k] = 0.f; }
+      for (int k = 0; k < kDPerF; ++k) { ga[k] = 0.f; gb[k] = 0.f; }
       for (int i = i0; i < i1; ++i) {
         const float4 r = tile[i];
 #pragma unroll
-        for (int k = 0; k < kDPer; ++k) {
+        for (int k = 0; k < kDPerF; ++k) {
           float s, c;
           phase_sincos(tq[k], r, &s, &c);
           ga[k] = fmaf(r.w, c, ga[k]);
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restri
         }
       }
 #pragma unroll
-      for (int k = 0; k < kDPer; ++k) {
+      for (int k = 0; k < kDPerF; ++k) {
         // compensated additions (round-to-nearest intrinsics: not contracted)
         const float ya = __fsub_rn(ga[k], ca[k]);
         const float ta = __fadd_rn(pa[k], ya);
@@ -145,13 +148,13 @@ __global__ void __launch_bounds__(kDThreads) k_direct_fwd(const float4* __restri
       }
     }
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) {
+    for (int k = 0; k < kDPerF; ++k) {
       A[k] += (double)pa[k] - (double)ca[k];
       B[k] += (double)pb[k] - (double)cb[k];
     }
   }
 #pragma unroll
-  for (int k = 0; k < kDPer; ++k) {
+  for (int k = 0; k < kDPerF; ++k) {
     if (qi[k] < n_q) {
       const int64_t o = sys * n_q + qi[k];
       S[o] = (float)(A[k] * A[k] + B[k] * B[k]);
@@ -170,12 +173,12 @@ __global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restri
   const int sys = blockIdx.y;
   const float4* R = rf + sys * n_atoms;
   const float4* Q = q + sys * q_sys_stride;
-  float4 r[kDPer];
-  int64_t ai[kDPer];
-  double gx[kDPer], gy[kDPer], gz[kDPer], gf[kDPer];
+  float4 r[kDPerB];
+  int64_t ai[kDPerB];
+  double gx[kDPerB], gy[kDPerB], gz[kDPerB], gf[kDPerB];
 #pragma unroll
-  for (int k = 0; k < kDPer; ++k) {
-    ai[k] = (int64_t)blockIdx.x * kDThreads * kDPer + k * kDThreads + threadIdx.x;
+  for (int k = 0; k < kDPerB; ++k) {
+    ai[k] = (int64_t)blockIdx.x * kDThreads * kDPerB + k * kDThreads + threadIdx.x;
     r[k] = ai[k] < n_atoms ? __ldg(R + ai[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
     gx[k] = gy[k] = gz[k] = gf[k] = 0.0;
   }
@@ -191,15 +194,15 @@ __global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restri
       tg[i] = make_float2(gg * ab.x, gg * ab.y);
     }
     __syncthreads();
-    float px[kDPer], py[kDPer], pz[kDPer], pf[kDPer];
+    float px[kDPerB], py[kDPerB], pz[kDPerB], pf[kDPerB];
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) px[k] = py[k] = pz[k] = pf[k] = 0.f;
+    for (int k = 0; k < kDPerB; ++k) px[k] = py[k] = pz[k] = pf[k] = 0.f;
     for (int i = 0; i < nq; ++i) {
       const QTurns t = tq[i];
       const float4 qq = tqr[i];
       const float2 ga = tg[i];
 #pragma unroll
-      for (int k = 0; k < kDPer; ++k) {
+      for (int k = 0; k < kDPerB; ++k) {
         float s, c;
         phase_sincos(t, r[k], &s, &c);
         const float w = fmaf(ga.y, c, -ga.x * s);   // gB cos - gA sin
@@ -210,12 +213,12 @@ __global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restri
       }
     }
 #pragma unroll
-    for (int k = 0; k < kDPer; ++k) {
+    for (int k = 0; k < kDPerB; ++k) {
       gx[k] += (double)px[k]; gy[k] += (double)py[k]; gz[k] += (double)pz[k]; gf[k] += (double)pf[k];
     }
   }
 #pragma unroll
-  for (int k = 0; k < kDPer; ++k) {
+  for (int k = 0; k < kDPerB; ++k) {
     if (ai[k] < n_atoms) {
       const double f2 = 2.0 * (double)r[k].w;
       grad[sys * n_atoms + ai[k]] =
@@ -235,7 +238,7 @@ int msf_direct_fwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
   if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
   if (n_q == 0) return MSF_OK;
   if (!q || !S || !AB || (n_atoms > 0 && !r_f)) return MSF_E_INVALID;
-  const int64_t per = (int64_t)kDThreads * kDPer;
+  const int64_t per = (int64_t)kDThreads * kDPerF;
   const int64_t nb = (n_q + per - 1) / per;
   if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
   dim3 grid((unsigned)nb, n_sys);
@@ -251,7 +254,7 @@ int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
   if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
   if (n_atoms == 0) return MSF_OK;
   if (!r_f || !grad || (n_q > 0 && (!q || !g || !AB))) return MSF_E_INVALID;
-  const int64_t per = (int64_t)kDThreads * kDPer;
+  const int64_t per = (int64_t)kDThreads * kDPerB;
   const int64_t nb = (n_atoms + per - 1) / per;
   if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
   dim3 grid((unsigned)nb, n_sys);
