@@ -56,12 +56,13 @@ WORKLOAD = ("columnar 200k atoms, 16.0x13.856x8.0 nm, 256x256x128 grid, 100 fram
             "get_dplot + Ewald lambda=0.154 nm")
 # source-level FP32 operation counts of one (atom, q) pair of the direct sum
 # (msf_direct.cu): the phase in turns from hi + lo parts of q/2pi with FMA
-# residuals (3 x [FMUL, 2 FFMA, FRND, 2 FADD], 2 FADD, FRND + FADD), the
-# turn-based sin/cos (FMUL, FRND, FFMA, FMUL, 4 + 4 polynomial FMA/FMUL,
-# F2I, LOP, 2 selects, 2 sign selects: 17), then the accumulation (forward:
-# 2 FFMA and the grouped compensated sum, ~0.5 per pair; adjoint: the
-# weight, 3 gradient and 2 weight-gradient FMAs: 7)
-DIRECT_FP32_OPS = {"fwd": 41.5, "bwd": 46}
+# residuals (3 x [FMUL, 2 FFMA, FRND, 2 FADD], 2 FADD), the turn-based
+# sin/cos whose quadrant rounding also removes the whole turns (FMUL, FRND,
+# FFMA, FMUL, 4 + 4 polynomial FMA/FMUL, F2I, LOP, 2 selects, 2 sign selects:
+# 17), then the accumulation (forward: 2 FFMA and the grouped compensated
+# sum, ~0.5 per pair; adjoint: the weight, 3 gradient and 2 weight-gradient
+# FMAs: 7)
+DIRECT_FP32_OPS = {"fwd": 39.5, "bwd": 44}
 SM_COUNT_FALLBACK = 152
 FP32_LANES_PER_SM = 128
 
