@@ -816,9 +816,26 @@ def direct_extra(torch, dev, keep=None):
         f"ceiling at {mhz:.0f} MHz x {sms} SMs: FP32 issue = 128 lanes/SM / FP32 ops per pair "
         f"({DIRECT_FP32_OPS['fwd']} forward, {DIRECT_FP32_OPS['bwd']} adjoint, source-level count; sin/cos are "
         f"polynomials in turns on the FP32 pipe, no SFU)")
+    # one system alone (config 4's base case): the kernels switch to smaller
+    # blocks so that 20k atoms / 65,536 q still cover the SMs
+    r1 = r[0].clone().requires_grad_(True)
+    f1, t1 = f[0], target[0]
+
+    def one():
+        S1 = mdsf.direct_sf(r1, f1, q)
+        l1 = torch.mean((torch.log1p(S1) - torch.log1p(t1)) ** 2)
+        return torch.autograd.grad(l1, r1)[0]
+    one()
+    torch.cuda.synchronize()
+    e[0].record()
+    for _ in range(reps):
+        one()
+    e[1].record()
+    torch.cuda.synchronize()
+    res["grad_evals_single_system_per_s"] = reps / (e[0].elapsed_time(e[1]) / 1000.0)
     if keep is not None:
         keep["_direct_S"] = (rs[0], fs[0], q_np, S[0].detach().cpu().numpy().astype(np.float64))
-    del r, f, q, rr, S, g, target
+    del r, f, q, rr, S, g, target, r1
     torch.cuda.empty_cache()
     return res
 

@@ -93,19 +93,20 @@ __device__ __forceinline__ void phase_sincos(const QTurns& q, float4 r, float* s
   sincos_turns(t, s, c);
 }
 
-__global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
-                                                          const float4* __restrict__ q, int64_t n_q,
-                                                          int64_t q_sys_stride, float* S, float2* AB) {
+template <int NTH, int PER>
+__global__ void __launch_bounds__(NTH, 2) k_direct_fwd(const float4* __restrict__ rf, int64_t n_atoms,
+                                                      const float4* __restrict__ q, int64_t n_q,
+                                                      int64_t q_sys_stride, float* S, float2* AB) {
   __shared__ float4 tile[kDTile];
   const int sys = blockIdx.y;
   const float4* R = rf + sys * n_atoms;
   const float4* Q = q + sys * q_sys_stride;
-  QTurns tq[kDPerF];
-  int64_t qi[kDPerF];
-  double A[kDPerF], B[kDPerF];
+  QTurns tq[PER];
+  int64_t qi[PER];
+  double A[PER], B[PER];
 #pragma unroll
-  for (int k = 0; k < kDPerF; ++k) {
-    qi[k] = (int64_t)blockIdx.x * kDThreads * kDPerF + k * kDThreads + threadIdx.x;
+  for (int k = 0; k < PER; ++k) {
+    qi[k] = (int64_t)blockIdx.x * NTH * PER + k * NTH + threadIdx.x;
     float4 v = qi[k] < n_q ? __ldg(Q + qi[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
     tq[k] = q_turns(v);
     A[k] = 0.0; B[k] = 0.0;
@@ -113,21 +114,21 @@ __global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __res
   for (int64_t a0 = 0; a0 < n_atoms; a0 += kDTile) {
     const int na = (int)min((int64_t)kDTile, n_atoms - a0);
     __syncthreads();
-    for (int i = threadIdx.x; i < na; i += kDThreads) tile[i] = __ldg(R + a0 + i);
+    for (int i = threadIdx.x; i < na; i += NTH) tile[i] = __ldg(R + a0 + i);
     __syncthreads();
     // tile partials with their Kahan compensations
-    float pa[kDPerF], pb[kDPerF], ca[kDPerF], cb[kDPerF];
+    float pa[PER], pb[PER], ca[PER], cb[PER];
 #pragma unroll
-    for (int k = 0; k < kDPerF; ++k) { pa[k] = 0.f; pb[k] = 0.f; ca[k] = 0.f; cb[k] = 0.f; }
+    for (int k = 0; k < PER; ++k) { pa[k] = 0.f; pb[k] = 0.f; ca[k] = 0.f; cb[k] = 0.f; }
     for (int i0 = 0; i0 < na; i0 += kDGroup) {
       const int i1 = min(i0 + kDGroup, na);
-      float ga[kDPerF], gb[kDPerF];
+      float ga[PER], gb[PER];
 #pragma unroll
-      for (int k = 0; k < kDPerF; ++k) { ga[k] = 0.f; gb[k] = 0.f; }
+      for (int k = 0; k < PER; ++k) { ga[k] = 0.f; gb[k] = 0.f; }
       for (int i = i0; i < i1; ++i) {
         const float4 r = tile[i];
 #pragma unroll
-        for (int k = 0; k < kDPerF; ++k) {
+        for (int k = 0; k < PER; ++k) {
           float s, c;
           phase_sincos(tq[k], r, &s, &c);
           ga[k] = fmaf(r.w, c, ga[k]);
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __res
         }
       }
 #pragma unroll
-      for (int k = 0; k < kDPerF; ++k) {
+      for (int k = 0; k < PER; ++k) {
         // compensated additions (round-to-nearest intrinsics: not contracted)
         const float ya = __fsub_rn(ga[k], ca[k]);
         const float ta = __fadd_rn(pa[k], ya);
@@ -148,13 +149,13 @@ __global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __res
       }
     }
 #pragma unroll
-    for (int k = 0; k < kDPerF; ++k) {
+    for (int k = 0; k < PER; ++k) {
       A[k] += (double)pa[k] - (double)ca[k];
       B[k] += (double)pb[k] - (double)cb[k];
     }
   }
 #pragma unroll
-  for (int k = 0; k < kDPerF; ++k) {
+  for (int k = 0; k < PER; ++k) {
     if (qi[k] < n_q) {
       const int64_t o = sys * n_q + qi[k];
       S[o] = (float)(A[k] * A[k] + B[k] * B[k]);
@@ -163,29 +164,30 @@ __global__ void __launch_bounds__(kDThreads, 2) k_direct_fwd(const float4* __res
   }
 }
 
-__global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restrict__ rf, int64_t n_atoms,
-                                                          const float4* __restrict__ q, int64_t n_q,
-                                                          int64_t q_sys_stride, const float* __restrict__ g,
-                                                          const float2* __restrict__ AB, float4* grad) {
+template <int NTH, int PER>
+__global__ void __launch_bounds__(NTH) k_direct_bwd(const float4* __restrict__ rf, int64_t n_atoms,
+                                                   const float4* __restrict__ q, int64_t n_q,
+                                                   int64_t q_sys_stride, const float* __restrict__ g,
+                                                   const float2* __restrict__ AB, float4* grad) {
   __shared__ QTurns tq[kDTile];   // q/2pi as hi + lo
   __shared__ float4 tqr[kDTile];  // q (rad)
   __shared__ float2 tg[kDTile];   // (g*A, g*B)
   const int sys = blockIdx.y;
   const float4* R = rf + sys * n_atoms;
   const float4* Q = q + sys * q_sys_stride;
-  float4 r[kDPerB];
-  int64_t ai[kDPerB];
-  double gx[kDPerB], gy[kDPerB], gz[kDPerB], gf[kDPerB];
+  float4 r[PER];
+  int64_t ai[PER];
+  double gx[PER], gy[PER], gz[PER], gf[PER];
 #pragma unroll
-  for (int k = 0; k < kDPerB; ++k) {
-    ai[k] = (int64_t)blockIdx.x * kDThreads * kDPerB + k * kDThreads + threadIdx.x;
+  for (int k = 0; k < PER; ++k) {
+    ai[k] = (int64_t)blockIdx.x * NTH * PER + k * NTH + threadIdx.x;
     r[k] = ai[k] < n_atoms ? __ldg(R + ai[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
     gx[k] = gy[k] = gz[k] = gf[k] = 0.0;
   }
   for (int64_t q0 = 0; q0 < n_q; q0 += kDTile) {
     const int nq = (int)min((int64_t)kDTile, n_q - q0);
     __syncthreads();
-    for (int i = threadIdx.x; i < nq; i += kDThreads) {
+    for (int i = threadIdx.x; i < nq; i += NTH) {
       const float4 v = __ldg(Q + q0 + i);
       tqr[i] = v;
       tq[i] = q_turns(v);
@@ -194,15 +196,15 @@ __global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restri
       tg[i] = make_float2(gg * ab.x, gg * ab.y);
     }
     __syncthreads();
-    float px[kDPerB], py[kDPerB], pz[kDPerB], pf[kDPerB];
+    float px[PER], py[PER], pz[PER], pf[PER];
 #pragma unroll
-    for (int k = 0; k < kDPerB; ++k) px[k] = py[k] = pz[k] = pf[k] = 0.f;
+    for (int k = 0; k < PER; ++k) px[k] = py[k] = pz[k] = pf[k] = 0.f;
     for (int i = 0; i < nq; ++i) {
       const QTurns t = tq[i];
       const float4 qq = tqr[i];
       const float2 ga = tg[i];
 #pragma unroll
-      for (int k = 0; k < kDPerB; ++k) {
+      for (int k = 0; k < PER; ++k) {
         float s, c;
         phase_sincos(t, r[k], &s, &c);
         const float w = fmaf(ga.y, c, -ga.x * s);   // gB cos - gA sin
@@ -213,18 +215,31 @@ __global__ void __launch_bounds__(kDThreads) k_direct_bwd(const float4* __restri
       }
     }
 #pragma unroll
-    for (int k = 0; k < kDPerB; ++k) {
+    for (int k = 0; k < PER; ++k) {
       gx[k] += (double)px[k]; gy[k] += (double)py[k]; gz[k] += (double)pz[k]; gf[k] += (double)pf[k];
     }
   }
 #pragma unroll
-  for (int k = 0; k < kDPerB; ++k) {
+  for (int k = 0; k < PER; ++k) {
     if (ai[k] < n_atoms) {
       const double f2 = 2.0 * (double)r[k].w;
       grad[sys * n_atoms + ai[k]] =
           make_float4((float)(f2 * gx[k]), (float)(f2 * gy[k]), (float)(f2 * gz[k]), (float)(2.0 * gf[k]));
     }
   }
+}
+
+// multiprocessor count of the current device (cached per device)
+static int sm_count() {
+  static int cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cache[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = n > 0 ? n : 152;
+  }
+  return cache[dev];
 }
 
 }  // namespace msf
@@ -238,13 +253,23 @@ int msf_direct_fwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
   if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
   if (n_q == 0) return MSF_OK;
   if (!q || !S || !AB || (n_atoms > 0 && !r_f)) return MSF_E_INVALID;
-  const int64_t per = (int64_t)kDThreads * kDPerF;
-  const int64_t nb = (n_q + per - 1) / per;
-  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
-  dim3 grid((unsigned)nb, n_sys);
-  k_direct_fwd<<<grid, kDThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      static_cast<const float4*>(r_f), n_atoms, static_cast<const float4*>(q), n_q,
-      q_shared ? 0 : n_q, S, static_cast<float2*>(AB));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const float4* rp = static_cast<const float4*>(r_f);
+  const float4* qp = static_cast<const float4*>(q);
+  const int64_t qs = q_shared ? 0 : n_q;
+  // few systems: one q per thread in 128-thread blocks, so that the blocks
+  // still cover the SMs (the 4-per-thread form needs n_q/1024 * n_sys of them)
+  const int64_t nb_big = (n_q + kDThreads * kDPerF - 1) / (kDThreads * kDPerF);
+  if (nb_big * n_sys >= 2 * (int64_t)sm_count()) {
+    if (nb_big > 0x7fffffff) return MSF_E_UNSUPPORTED;
+    k_direct_fwd<kDThreads, kDPerF><<<dim3((unsigned)nb_big, n_sys), kDThreads, 0, st>>>(
+        rp, n_atoms, qp, n_q, qs, S, static_cast<float2*>(AB));
+  } else {
+    const int64_t nb = (n_q + 127) / 128;
+    if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
+    k_direct_fwd<128, 1><<<dim3((unsigned)nb, n_sys), 128, 0, st>>>(rp, n_atoms, qp, n_q, qs, S,
+                                                                     static_cast<float2*>(AB));
+  }
   return launch_status();
 }
 
@@ -254,13 +279,22 @@ int msf_direct_bwd(const void* r_f, int64_t n_atoms, const void* q, int64_t n_q,
   if (n_atoms < 0 || n_q < 0 || n_sys < 1 || n_sys > 65535) return MSF_E_INVALID;
   if (n_atoms == 0) return MSF_OK;
   if (!r_f || !grad || (n_q > 0 && (!q || !g || !AB))) return MSF_E_INVALID;
-  const int64_t per = (int64_t)kDThreads * kDPerB;
-  const int64_t nb = (n_atoms + per - 1) / per;
-  if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
-  dim3 grid((unsigned)nb, n_sys);
-  k_direct_bwd<<<grid, kDThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      static_cast<const float4*>(r_f), n_atoms, static_cast<const float4*>(q), n_q,
-      q_shared ? 0 : n_q, g, static_cast<const float2*>(AB), static_cast<float4*>(grad));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const float4* rp = static_cast<const float4*>(r_f);
+  const float4* qp = static_cast<const float4*>(q);
+  const int64_t qs = q_shared ? 0 : n_q;
+  // few systems: one atom per thread in 64-thread blocks (more blocks over the SMs)
+  const int64_t nb_big = (n_atoms + kDThreads * kDPerB - 1) / (kDThreads * kDPerB);
+  if (nb_big * n_sys >= 2 * (int64_t)sm_count()) {
+    if (nb_big > 0x7fffffff) return MSF_E_UNSUPPORTED;
+    k_direct_bwd<kDThreads, kDPerB><<<dim3((unsigned)nb_big, n_sys), kDThreads, 0, st>>>(
+        rp, n_atoms, qp, n_q, qs, g, static_cast<const float2*>(AB), static_cast<float4*>(grad));
+  } else {
+    const int64_t nb = (n_atoms + 63) / 64;
+    if (nb > 0x7fffffff) return MSF_E_UNSUPPORTED;
+    k_direct_bwd<64, 1><<<dim3((unsigned)nb, n_sys), 64, 0, st>>>(
+        rp, n_atoms, qp, n_q, qs, g, static_cast<const float2*>(AB), static_cast<float4*>(grad));
+  }
   return launch_status();
 }
 
