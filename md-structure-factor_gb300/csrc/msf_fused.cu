@@ -217,13 +217,18 @@ struct PlaneShape {
 //     the other's partner, both outputs;
 //   edge line, k1 = 0 and B/2: two self-paired items in one unit.
 // That is B*n2/2 units of equal transform work: exactly two per thread at
-// the headline size, with no tail.  Edge units come first.
+// the headline size, with no tail.  Unit u takes slot (k1 = u / (n2/2),
+// l = u % (n2/2)): consecutive threads walk l with k1 fixed, so k1 -- and with
+// it the twiddle index w^q, q = k1 + B*k2 -- is uniform across a warp when
+// n2/2 is a multiple of 32 (one constant-cache access per twiddle), and the
+// B slots with l = 0 hold the 2 x B/2 edge units (line 0 for k1 < B/2, line
+// n2/2 for the others), one per warp pair instead of all in warp 0.
 template <int N1, int N2, int SP, int NT, bool ZERO = false, bool PAIRS = false>
 __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   constexpr int P = N1 / 2, NH = N2 / 2 + 1;
   constexpr int A = r2::Split2<P>::A, B = r2::Split2<P>::B;
-  constexpr int KM = N2 / 2 - 1;          // interior output lines 1 .. n2/2 - 1
-  constexpr int U = B * (N2 / 2);         // B edge units + B*KM interior units
+  constexpr int H = N2 / 2;               // interior output lines 1 .. H - 1
+  constexpr int U = B * H;                // B edge units + B*(H - 1) interior units
   const CTw<N1> wq;
   auto emit = [&](int q, int k, float2 w, float2 wm_raw) {
     const float2 wm = cconj(wm_raw);
@@ -235,13 +240,15 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   };
   for (int u = threadIdx.x; u < U; u += NT) {
     int l, lp, k1, k1p;
-    if (u < B) {                     // edge line: j = 0 pairs the two self-paired items
-      l = lp = u < B / 2 ? 0 : N2 / 2;
-      k1 = u % (B / 2);
+    const int kk = u / H, ll = u % H;
+    const bool edge = ll == 0;
+    if (edge) {                      // edge line: k1 = 0 pairs the two self-paired items
+      l = lp = kk < B / 2 ? 0 : N2 / 2;
+      k1 = kk % (B / 2);
       k1p = k1 ? B - k1 : B / 2;
     } else {
-      k1 = (u - B) / KM;
-      l = 1 + (u - B) % KM;
+      k1 = kk;
+      l = ll;
       lp = N2 - l;
       k1p = (B - k1) & (B - 1);
     }
@@ -273,7 +280,7 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
     }
     reg::reg_dft<A>(a);
     reg::reg_dft<A>(b);
-    if (u < B && k1 == 0) {
+    if (edge && k1 == 0) {
 #pragma unroll
       for (int k2 = 0; k2 < A; ++k2) emit(B * k2, l, a[k2], a[(A - k2) & (A - 1)]);
 #pragma unroll
@@ -284,7 +291,7 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
     } else {
 #pragma unroll
       for (int k2 = 0; k2 < A; ++k2) emit(k1 + B * k2, l, a[k2], b[A - 1 - k2]);
-      if (u < B) {
+      if (edge) {
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2) emit(k1p + B * k2, l, b[k2], a[A - 1 - k2]);
       }
