@@ -18,8 +18,10 @@
 //                    fused with the 2-D real split
 //                      E = (W[q,k] + conj W[-q,-k])/2, O = (W[q,k] - conj W[-q,-k])/(2i)
 //                      Y[q,k] = E + w^q O, Y[q+P,k] = E - w^q O   (w = e^{-2 pi i/n1})
-//                    written as the (n1, n2/2+1) half plane.  The density grid
-//                    never goes to global memory.
+//                    written as the (n1, n2/2+1) half plane; the weights are
+//                    deposited halved (exact in FP32), which takes the 1/2
+//                    out of E and O.  The density grid never goes to global
+//                    memory.
 //   k_xpower_tma     (msf_xtma.cu; k_xpower_ct without TMA) x-FFT of W spectrum
 //                    columns for every frame of the batch, |F|^2 summed over
 //                    the batch in FP32, one FP64 RMW of sf every kPowerFlush
@@ -230,10 +232,11 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   constexpr int H = N2 / 2;               // interior output lines 1 .. H - 1
   constexpr int U = B * H;                // B edge units + B*(H - 1) interior units
   const CTw<N1> wq;
+  // the plane holds half the weights, so E and O need no factor 1/2
   auto emit = [&](int q, int k, float2 w, float2 wm_raw) {
     const float2 wm = cconj(wm_raw);
-    const float2 E = cscale(cadd(w, wm), 0.5f);
-    const float2 O = cscale(cmi(csub(w, wm)), 0.5f);
+    const float2 E = cadd(w, wm);
+    const float2 O = cmi(csub(w, wm));
     const float2 t = cmul(wq(q), O);
     __stcs(out + q * NH + k, cadd(E, t));   // evict-first: keep L2 for the bucket entries
     __stcs(out + (q + P) * NH + k, csub(E, t));
@@ -352,7 +355,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
     if (a.grid_kind == kGridI32) v = (float)__ldg(static_cast<const int32_t*>(a.grids) + g0 + e);
     else if (a.grid_kind == kGridF32) v = __ldg(static_cast<const float*>(a.grids) + g0 + e);
     else v = (float)__ldg(static_cast<const double*>(a.grids) + g0 + e);
-    buff[pair_offset<N2, SP>(e)] = v;
+    buff[pair_offset<N2, SP>(e)] = 0.5f * v;   // halved: the split's 1/2 (exact)
   }
   __syncthreads();
   plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
@@ -369,7 +372,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
 // returns.  With a.stall (the plan's diagnostic option) the
 // first wait expects 16 bytes that no copy delivers, so it runs out: the
 // error path can be tested without any fault.
-constexpr int kPlanePrefetch = 2;
+constexpr int kPlanePrefetch = 3;
 
 template <int N1, int N2>
 struct BucketPlaneShape {
@@ -457,13 +460,14 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     }
     phase ^= 1u;
     // integer weights summed in FP32: exact (and order-independent) while a
-    // voxel's total stays below 2^24 electrons
+    // voxel's total stays below 2^24 electrons; deposited halved, which is
+    // exact too and takes the split's factor 1/2
     {
       const int n = ctl[1], ns = n < CAP ? n : CAP;
       const int2* src = a.pbucket + (int64_t)frame * a.pstride + ctl[0];
       for (int e = tid; e < n; e += NT) {
         const int2 v = e < ns ? staged[e] : src[e];
-        atomicAdd(buff + pair_offset<N2, SP>(v.x), (float)v.y);
+        atomicAdd(buff + pair_offset<N2, SP>(v.x), 0.5f * (float)v.y);
       }
     }
     __syncthreads();   // staging area and the range consumed

@@ -43,8 +43,10 @@ __device__ __forceinline__ void pass1_fn(float2* s, TW tw) {
 #pragma unroll
       for (int n2 = 0; n2 < B; ++n2) v[n2] = p[n2 * A * SM];
       reg::reg_dft<B>(v);
+      if (n1 != 0) {   // n1 = 0: every twiddle is 1
 #pragma unroll
-      for (int k1 = 1; k1 < B; ++k1) v[k1] = cmul(v[k1], tw(n1 * k1));
+        for (int k1 = 1; k1 < B; ++k1) v[k1] = cmul(v[k1], tw(n1 * k1));
+      }
 #pragma unroll
       for (int k1 = 0; k1 < B; ++k1) p[k1 * A * SM] = v[k1];
     }
@@ -242,11 +244,12 @@ __device__ __forceinline__ void pass1_samplepairs(float2* s, TW tw) {
       for (int n2 = 0; n2 < B; ++n2) ld2(p + n2 * A, u[n2], v[n2]);
       reg::reg_dft<B>(u);
       reg::reg_dft<B>(v);
+      if (n1 != 0) {   // n1 = 0 (whole warps when NL >= 32): u's twiddles are 1
 #pragma unroll
-      for (int k1 = 1; k1 < B; ++k1) {
-        u[k1] = cmul(u[k1], tw(n1 * k1));
-        v[k1] = cmul(v[k1], tw((n1 + 1) * k1));
+        for (int k1 = 1; k1 < B; ++k1) u[k1] = cmul(u[k1], tw(n1 * k1));
       }
+#pragma unroll
+      for (int k1 = 1; k1 < B; ++k1) v[k1] = cmul(v[k1], tw((n1 + 1) * k1));
 #pragma unroll
       for (int k1 = 0; k1 < B; ++k1) st2(p + k1 * A, u[k1], v[k1]);
     }

@@ -94,6 +94,19 @@ __host__ __device__ constexpr float2 w64(int k) {
 template <int R>
 __host__ __device__ __forceinline__ float2 wr(int m) { return w64((m % R) * (64 / R)); }
 
+// v * w_R^m with m a constant once unrolled: the quarter turns are a swap
+// and sign changes (a product with the 0 of w = -i would cost an FMA: x * 0
+// is not folded without fast math)
+template <int R>
+__host__ __device__ __forceinline__ float2 twiddle(float2 v, int m) {
+  m %= R;
+  if (m == 0) return v;
+  if (4 * m == R) return cmi(v);
+  if (2 * m == R) return make_float2(-v.x, -v.y);
+  if (4 * m == 3 * R) return cpi(v);
+  return cmul(v, wr<R>(m));
+}
+
 template <int R> struct Split {
   static constexpr int A = (R == 16) ? 4 : ((R == 32) ? 4 : 8);   // R = A * B
   static constexpr int B = R / A;
@@ -113,8 +126,7 @@ __host__ __device__ __forceinline__ void reg_dft(float2* a) {
       for (int n2 = 0; n2 < B; ++n2) y[n1][n2] = a[n1 + A * n2];
       reg_dft<B>(y[n1]);
 #pragma unroll
-      for (int k1 = 1; k1 < B; ++k1)
-        if (n1 * k1) y[n1][k1] = cmul(y[n1][k1], wr<R>(n1 * k1));
+      for (int k1 = 1; k1 < B; ++k1) y[n1][k1] = twiddle<R>(y[n1][k1], n1 * k1);
     }
 #pragma unroll
     for (int k1 = 0; k1 < B; ++k1) {
