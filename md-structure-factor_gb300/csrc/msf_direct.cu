@@ -73,15 +73,20 @@ __device__ __forceinline__ float turn_frac(float hi, float lo, float r) {
 __device__ __forceinline__ void sincos_turns(float t, float* s, float* c) {
   // t in [-3/2, 3/2]: the quadrant k = rint(4t) (|k| <= 6) also takes off
   // the whole turns, and t - k/4 is exact (Sterbenz: t and k/4 are within a
-  // factor 2 of each other for k != 0); only k mod 4 matters below
-  const float k = rintf(4.0f * t);
+  // factor 2 of each other for k != 0); only k mod 4 matters below.  k is
+  // rounded by adding 1.5 * 2^23 (the sum's unit is 1, so the FMA rounds 4t
+  // to the nearest integer, ties to even, like rintf): the sum's low bits
+  // then hold k mod 4 and no float-to-int conversion is needed
+  constexpr float kRound = 12582912.0f;
+  const float kb = fmaf(4.0f, t, kRound);
+  const float k = kb - kRound;
   const float r = fmaf(-0.25f, k, t);
   const float z = r * r;
   const float ps = r * fmaf(fmaf(fmaf(-75.40099585508018f, z, 81.5925250459675f), z, -41.34166242174424f), z,
                             6.283185287502589f);
   const float pc = fmaf(fmaf(fmaf(fmaf(59.22042251089335f, z, -85.44285258833072f), z, 64.9393162129225f), z,
                              -19.73920865037173f), z, 0.9999999999526074f);
-  const int q = (int)k & 3;
+  const int q = __float_as_int(kb) & 3;
   const float sv = (q & 1) ? pc : ps;
   const float cv = (q & 1) ? ps : pc;
   *s = (q >= 2) ? -sv : sv;                 // quadrants 2, 3
