@@ -330,7 +330,7 @@ def resolve_tuning(args, dev):
     source = "autotuner cache"
     t0 = time.perf_counter()
     if tune.lookup(DIMS) is None:
-        tune.tune(DIMS, n_atoms=N_ATOMS, frames=64, device=dev)
+        tune.tune(DIMS, n_atoms=N_ATOMS, frames=128, device=dev)
         source = "autotuned at start-up"
     e = tune.entry(DIMS)
     rec = {"source": source, "cache_key": tune.key(DIMS), "cache": tune.cache_path(),

@@ -165,6 +165,7 @@ struct PlaneCtArgs {
   const int* poff;
   int64_t pstride;
   int* status;
+  int* next_item;         // plane hand-out counter, zeroed before each launch
   long long wait_limit;   // bounded-wait limit (polls)
   int stall;          // MSF_PLAN_DIAG_STALL: arm the first wait for a copy never issued
   // output
@@ -361,8 +362,13 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 80))) k_plane_grid(PlaneC
   plane_transform<N1, N2>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
 }
 
-// Bucket source, persistent: CTA b transforms planes (frame, x) = item b,
-// b + gridDim.x, ... of the batch.  A plane's atoms are one contiguous, even
+// Bucket source, persistent: CTA b transforms plane (frame, x) = item b
+// first, then the planes a global counter hands out (items gridDim.x, ...,
+// in the order asked for): a CTA that starts late -- its SM still held by the
+// CTAs of the x pass running beside on another stream -- takes fewer planes
+// instead of holding the launch up.  With a fixed share per CTA, runs where
+// x-pass CTAs had doubled up on some SMs when the plane kernel started took
+// 30.5 instead of 23.8 us per frame.  A plane's atoms are one contiguous, even
 // range of the compacted entries (k_bucket_compact); thread 0 fetches up to
 // kPlanePrefetch*NT of them into shared memory with one cp.async.bulk copy
 // tracked by an mbarrier, issued before the FFT of the previous plane, so the
@@ -400,15 +406,17 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
   float* buff = reinterpret_cast<float*>(buf);
   int2* staged = reinterpret_cast<int2*>(buf + N2 * SP);    // CAP entries
   uint64_t* bar = reinterpret_cast<uint64_t*>(staged + CAP);
-  int* ctl = reinterpret_cast<int*>(bar + 1);   // [0] range begin, [1] count, [2] abort flag
+  int* ctl = reinterpret_cast<int*>(bar + 1);   // [0] range begin, [1] count, [2] abort flag, [3] next plane
   const int tid = threadIdx.x;
   const int G = gridDim.x;
   // thread 0: offsets (begin, end) of plane `item` in the compacted entries,
-  // and the copy of its first CAP entries.  The offsets of the plane after
-  // next are loaded one plane ahead and first used a plane later: a count
-  // formed right after the load stalled thread 0 -- and with it warp 0 and
-  // every barrier after it -- for ~3k cycles per plane (measured with clock64
-  // stamps), the latency of a global load under the kernel's own traffic.
+  // and the copy of its first CAP entries.  The plane after next is fetched
+  // from the counter, and its offsets loaded, one plane ahead and first used
+  // a plane later: a count formed right after the load stalled thread 0 --
+  // and with it warp 0 and every barrier after it -- for ~3k cycles per plane
+  // (measured with clock64 stamps), the latency of a global load under the
+  // kernel's own traffic.
+  auto fetch = [&]() { return G + atomicAdd(a.next_item, 1); };
   auto range_raw = [&](int item) {
     const int frame = item / a.n0, x = item - frame * a.n0;
     const int* po = a.poff + (int64_t)frame * (a.n0 + 1) + x;
@@ -423,7 +431,8 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     mbar_expect_tx(bar, (uint32_t)ns * sizeof(int2));
     if (ns > 0) bulk_load(staged, a.pbucket + (int64_t)(item / a.n0) * a.pstride + r.x, ns * sizeof(int2), bar);
   };
-  int2 after = make_int2(0, 0);   // thread 0: offsets of the plane after the next
+  int2 after = make_int2(0, 0);   // thread 0: offsets of plane nxt
+  int nxt = items, nxt2 = items;  // thread 0: the next plane and the one after it
   int item = blockIdx.x;
   // the plane starts zeroed; afterwards the split of each plane clears what
   // it reads, so the next deposit finds it zeroed again
@@ -443,11 +452,15 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     }
     ctl[0] = r.x;
     ctl[1] = r.y;
-    if (item + G < items) after = range_raw(item + G);
+    nxt = fetch();
+    if (nxt < items) {
+      after = range_raw(nxt);
+      nxt2 = fetch();
+    }
   }
   __syncthreads();
   uint32_t phase = 0;
-  for (; item < items; item += G) {
+  while (item < items) {
     const int frame = item / a.n0, x = item - frame * a.n0;
     long long spins = 0;
     while (!mbar_try_wait(bar, phase)) {
@@ -472,7 +485,7 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
     }
     __syncthreads();   // staging area and the range consumed
     if (tid == 0) {
-      const int next = item + G;
+      const int next = nxt;
       const int2 r = make_int2(after.x, after.y - after.x);   // loaded a plane ago
       if (next < items) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -480,9 +493,15 @@ __global__ void __maxnreg__((MSF_PLANE_MAXNREG(N1, N2, 88))) k_plane_ct(PlaneCtA
       }
       ctl[0] = r.x;
       ctl[1] = r.y;
-      if (next + G < items) after = range_raw(next + G);
+      ctl[3] = next;
+      nxt = nxt2;                      // fetched a plane ago
+      if (nxt < items) {
+        after = range_raw(nxt);
+        nxt2 = fetch();
+      }
     }
     plane_transform<N1, N2, true>(buf, a.C + frame * a.Vh + (int64_t)x * N1 * S::NH);
+    item = ctl[3];   // written by thread 0 before the transform's barriers
   }
   // leave no copy in flight into this CTA's shared memory (bounded)
   if (tid == 0 && ctl[2]) {
@@ -574,6 +593,8 @@ static int launch_plane_ct(const PlaneCtArgs& a, int src, int n0, int nframes, c
   static int sms = 0;
   if (src == 0) {
     allow_smem_once(k_plane_ct<N1, N2>, once0, BucketPlaneShape<N1, N2>::SMEM);
+    const int ms = cuda_status(cudaMemsetAsync(a.next_item, 0, sizeof(int), st));
+    if (ms) return ms;
     if (!sms) {
       int dev = 0;
       cudaGetDevice(&dev);
@@ -833,6 +854,7 @@ static PlaneCtArgs plane_args(const msf_plan* p) {
   a.poff = ws_ptr<int>(p, p->off_poff);
   a.pstride = p->pstride;
   a.status = ws_ptr<int>(p, p->off_status);
+  a.next_item = ws_ptr<int>(p, p->off_pnext);
   a.wait_limit = p->wait_limit;
   a.stall = p->diag_stall;
   return a;

@@ -167,13 +167,19 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
                        : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
   if (p->variant == 3 && n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
   if (p->variant == 3 && p->overlap && (n_frames > p->batch || cont || p->chain_k > 0)) {
-    // batch b: bucket sort + plane FFT into spectrum buffer b%2 on `st`, the
-    // x pass of batch b on `side` (after that plane FFT), overlapping the
+    // batch b: bucket sort + plane FFT into spectrum buffer b%2 on `plane_st`,
+    // the x pass of batch b on `side` (after that plane FFT), overlapping the
     // plane FFT of batch b+1; the plane FFT of batch b+2 waits for the x pass
-    // of batch b before reusing its buffer; `st` finally joins `side`.  With
-    // MSF_CONTINUE the batch count carries over to the next call and the
-    // join is left to the call that ends the chain.
-    int s = MSF_OK;
+    // of batch b before reusing its buffer.  `plane_st` starts after the
+    // caller's prior work and the caller's stream waits for it at the
+    // end of every call (the positions have been read); it joins `side` at
+    // the end of the chain.  With MSF_CONTINUE the batch count carries over
+    // to the next call and that join is left to the call that ends the
+    // chain.
+    int s = cuda_status(cudaEventRecord(p->ev_fork, st));
+    if (!s) s = cuda_status(cudaStreamWaitEvent(p->plane_st, p->ev_fork, 0));
+    const cudaStream_t caller = st;
+    st = p->plane_st;
     int64_t k = p->chain_k;
     for (int64_t f = 0; f < n_frames && !s; f += p->batch, ++k) {
       const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
@@ -189,13 +195,15 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
       if (!s) s = fused_x_batch(p, nb, sf, p->side, buf, !cont && f + nb >= n_frames);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_x[buf], p->side));
     }
+    if (!s) s = cuda_status(cudaEventRecord(p->ev_plane_st, st));
+    if (!s) s = cuda_status(cudaStreamWaitEvent(caller, p->ev_plane_st, 0));
     if (cont && !s) {
       p->chain_k = k;
       return MSF_OK;
     }
     p->chain_k = 0;
     // join: every x pass (recorded in order on `side`) precedes the last event
-    if (k >= 1 && !s) s = cuda_status(cudaStreamWaitEvent(st, p->ev_x[(k - 1) & 1], 0));
+    if (k >= 1 && !s) s = cuda_status(cudaStreamWaitEvent(caller, p->ev_x[(k - 1) & 1], 0));
     return s;
   }
   for (int64_t f = 0; f < n_frames; f += p->batch) {

@@ -68,18 +68,20 @@ struct msf_plan {
   // the entries compacted plane by plane (each plane's range padded to an
   // even count), the plane offsets, the per-plane counts (kept zero between
   // batches) and the per-plane placement cursors
-  size_t off_pbucket, off_poff, off_pcount, off_pcursor;
+  size_t off_pbucket, off_poff, off_pcount, off_pcursor, off_pnext;
   int64_t pstride;      // entries per frame in the compacted array
   // TMA tensor maps over the two spectrum buffers for the x pass (CUtensorMap, 128 bytes each)
   alignas(64) unsigned char xtma_map[2][128];
   int xtma_ready;
   // overlap (bucketed variant): spectra double-buffered, the x pass of one
-  // batch runs on `side` while the plane FFT of the next batch runs on the
-  // caller's stream; created by msf_plan_bind, released by plan_release
+  // batch runs on `side` while the bucket kernels and plane FFT of the next
+  // batch run on `plane_st`; both plan-owned streams of default priority,
+  // forked from the caller's stream (ev_fork) and joined back into it
+  // (ev_plane_st, ev_x).  Created by msf_plan_bind, released by plan_release
   int overlap;
   size_t off_cplx2;
-  cudaStream_t side;
-  cudaEvent_t ev_plane[2], ev_x[2];
+  cudaStream_t side, plane_st;
+  cudaEvent_t ev_plane[2], ev_x[2], ev_fork, ev_plane_st;
   // a chain continued over several calls (MSF_CONTINUE): batches issued so
   // far, for the spectrum-buffer parity and the reuse waits; 0 when joined
   int64_t chain_k;

@@ -3,9 +3,12 @@
 // The half spectra of a batch are one row-major matrix of B*n0 rows (frame,
 // x) by F = n1*(n2/2+1) complex columns.  A persistent CTA walks work items
 // (column tile of W columns, frame); each item's (n0 x W) tile is fetched by
-// cp.async.bulk.tensor.2d into one of two shared-memory buffers and tracked
-// by an mbarrier, so the copy of item s+1 (and s+2) runs while item s is
-// transformed.  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed
+// cp.async.bulk.tensor.2d into one of NS shared-memory buffers and tracked by
+// an mbarrier, so the copies of items s+1 .. s+NS-1 run while item s is
+// transformed (NS = 2: four buffers per 16 KB tile measured slower alone, as
+// they cost half the CTAs per SM).  Tiles of at most 2048 values take
+// 128-thread CTAs: beside a plane-FFT CTA (the overlapped launch) two of them
+// fit, alone six per SM.  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed
 // over the frames of the tile in FP32, one FP64 read-modify-write of sf per
 // tile every kPowerFlush frames and after the last.  Waits are bounded: on
 // timeout the kernel latches MSF_E_TIMEOUT in the plan status word and
@@ -27,35 +30,39 @@ struct XTmaArgs {
 
 template <int N0, int W>
 struct XTmaShape {
-  static constexpr int NT = 256;
+  static constexpr int NT = N0 * W >= 4096 ? 256 : 128;
   static constexpr int EPT = N0 * W / NT;
   static constexpr int BOX_ROWS = N0 <= 256 ? N0 : 256;
   static constexpr int NBOX = N0 / BOX_ROWS;
   static constexpr uint32_t TILE_BYTES = N0 * W * sizeof(float2);
-  static constexpr size_t SMEM = 1024 + 2 * (size_t)TILE_BYTES + N0 * sizeof(float2);
+  static constexpr int NS = 2;   // tile buffers
+  static constexpr size_t SMEM = 1024 + NS * (size_t)TILE_BYTES + N0 * sizeof(float2);
 };
 
+// register budget: 80 per thread, so that one 256-thread or two 128-thread
+// CTAs fit beside a plane-FFT CTA (512 threads x 88)
 template <int N0, int W>
-__global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_xpower_tma(const __grid_constant__ CUtensorMap map,
-                                                                       XTmaArgs a) {
+__global__ void __launch_bounds__(XTmaShape<N0, W>::NT,
+                                  (N0 <= 256 && N0 * W <= 4096 ? 3 * 256 / XTmaShape<N0, W>::NT : 1))
+    k_xpower_tma(const __grid_constant__ CUtensorMap map, XTmaArgs a) {
   using S = XTmaShape<N0, W>;
   constexpr int NT = S::NT, EPT = S::EPT;
   static_assert(EPT * NT == N0 * W, "tile must split evenly over the threads");
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar[2];
-  __shared__ int abort_flag;
+  constexpr int NS = S::NS;
+  __shared__ __align__(8) uint64_t bar[NS];
+  __shared__ int abort_flag, abort_at;
   // 1024-byte aligned tile buffers (TMA destination)
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   float2* buf0 = reinterpret_cast<float2*>(base);
-  float2* buf1 = buf0 + N0 * W;
-  float2* tw = buf1 + N0 * W;
+  float2* tw = buf0 + NS * N0 * W;
   const int tid = threadIdx.x;
   const int my_tiles = (a.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
   const int total = my_tiles > 0 ? my_tiles * a.nframes : 0;
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) mbar_init(&bar[k], 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -65,18 +72,16 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
   auto issue = [&](int s) {
     const int tile = (int)blockIdx.x + (s / a.nframes) * (int)gridDim.x;
     const int frame = s % a.nframes;
-    float2* dst = (s & 1) ? buf1 : buf0;
-    uint64_t* b = &bar[s & 1];
+    float2* dst = buf0 + (s % NS) * (N0 * W);
+    uint64_t* b = &bar[s % NS];
     mbar_expect_tx(b, S::TILE_BYTES);
 #pragma unroll
     for (int k = 0; k < S::NBOX; ++k)
       tma_load_2d(dst + k * S::BOX_ROWS * W, &map, tile * W, frame * N0 + k * S::BOX_ROWS, b);
   };
-  if (tid == 0) {
-    if (total > 0) issue(0);
-    if (total > 1) issue(1);
-  }
-  uint32_t phase0 = 0, phase1 = 0;
+  if (tid == 0)
+    for (int k = 0; k < NS && k < total; ++k) issue(k);
+  uint32_t phases = 0;   // bit k: parity of buffer k's next completion
   // pass-2 items (k1, column) owned by this thread; X[k1 + B*k2] power in acc
   constexpr int A = r2::Split2<N0>::A, B = r2::Split2<N0>::B;
   constexpr int ITEMS2 = B * W;
@@ -88,20 +93,23 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
     for (int k = 0; k < A; ++k) acc[j][k] = 0.f;
 
   for (int s = 0; s < total; ++s) {
-    const int b = s & 1;
+    const int b = s % NS;
     uint64_t* bb = &bar[b];
-    const uint32_t par = b ? phase1 : phase0;
+    const uint32_t par = (phases >> b) & 1u;
     long long spins = 0;
     while (!mbar_try_wait(bb, par)) {
       if (++spins > kWaitLimit) { atomicExch(&abort_flag, 1); break; }
     }
     __syncthreads();
     if (abort_flag) {
-      if (tid == 0) atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
+      if (tid == 0) {
+        atomicExch(a.status + kStatErr, MSF_E_TIMEOUT);
+        abort_at = s;
+      }
       break;
     }
-    if (b) phase1 ^= 1u; else phase0 ^= 1u;
-    float2* t = b ? buf1 : buf0;
+    phases ^= 1u << b;
+    float2* t = buf0 + b * (N0 * W);
     r2::pass1<N0, W, W, 1, NT>(t, tw);
     __syncthreads();
 #pragma unroll
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
         // in groups of 8: the group's loads first (independent), then the adds
         // and stores (a whole column of FP64 values would not fit the
         // register budget beside the accumulators)
-        constexpr int G8 = (W >= 16 && A > 8) ? 8 : A;
+        constexpr int G8 = A > 8 ? 8 : A;
 #pragma unroll
         for (int g = 0; g < A; g += G8) {
           double old[G8];
@@ -146,16 +154,19 @@ __global__ void __launch_bounds__(256, (N0 <= 256 && N0 * W <= 4096 ? 3 : 1)) k_
       }
     }
     __syncthreads();   // every thread is done with buffer b
-    if (tid == 0 && s + 2 < total) {
+    if (tid == 0 && s + NS < total) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(s + 2);
+      issue(s + NS);
     }
   }
-  // leave no copy in flight into this CTA's shared memory (bounded)
+  // leave no copy in flight into this CTA's shared memory (bounded): after an
+  // abort at item s the copies still owed are those of items s .. s + NS - 1
+  // (the ones issued), one per buffer
   if (tid == 0 && abort_flag) {
-    for (int k = 0; k < 2; ++k) {
+    for (int i = abort_at; i < abort_at + NS && i < total; ++i) {
+      const int k = i % NS;
       long long spins = 0;
-      while (!mbar_try_wait(&bar[k], k ? phase1 : phase0) && ++spins < kWaitLimit) {
+      while (!mbar_try_wait(&bar[k], (phases >> k) & 1u) && ++spins < kWaitLimit) {
       }
     }
   }
@@ -195,9 +206,9 @@ static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_xpower_tma<N0, W>, S::NT, S::SMEM);
     grid = (sms > 0 ? sms : 152) * (occ > 0 ? occ : 1);
   }
-  // beside a plane FFT: one CTA per SM (it co-resides with the plane CTA);
-  // alone: as many as fit
-  const int cap = (p->overlap && !alone) ? (sms > 0 ? sms : 152) : grid;
+  // beside a plane FFT: one 256-thread or two 128-thread CTAs per SM (they
+  // co-reside with the plane CTA); alone: as many as fit
+  const int cap = (p->overlap && !alone) ? (sms > 0 ? sms : 152) * (256 / S::NT) : grid;
   const int g = a.ntiles < cap ? a.ntiles : cap;
   k_xpower_tma<N0, W><<<g, S::NT, S::SMEM, st>>>(*map, a);
   return launch_status();

@@ -39,6 +39,7 @@ class Plan:
                              (C.c_double * 3)(*self.box), int(variant), int(tile_w),
                              int(rows_per_block), int(deposit_block), int(max_atoms), int(options))
         self.max_atoms = int(max_atoms)
+        self.options = int(options)
         h = c_p()
         call("msf_plan_create", C.byref(h), C.byref(desc))
         self._h = h
@@ -69,7 +70,8 @@ class Plan:
     def tuning(self):
         return dict(variant=VARIANTS[self.variant], tile_w=self.tile_w,
                     rows_per_block=self.rows_per_block, batch=self.batch,
-                    deposit_block=self.deposit_block, tma=self.tma)
+                    deposit_block=self.deposit_block, tma=self.tma,
+                    overlap=not (self.options & 1))
 
     def __del__(self):
         h = getattr(self, "_h", None)

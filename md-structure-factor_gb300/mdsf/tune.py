@@ -108,8 +108,9 @@ def _smooth(n):
 def candidates(dims):
     """Candidate tunings of a grid shape, the fused chains first.
 
-    Power-of-two grids: the bucketed chain with 16/32/64-frame batches and the
-    x tiles instantiated for n0, then the smooth chain.  2^a 3^b 5^c grids:
+    Power-of-two grids: the bucketed chain with 16/32/64-frame batches, the
+    x tiles instantiated for n0, and the x pass of one batch overlapped with
+    the next batch's plane FFT or not (``options=1``), then the smooth chain.  2^a 3^b 5^c grids:
     the smooth chain with 4-32-frame batches and 256/512-thread deposit
     blocks.  Other grids (a prime factor above 5, an odd n1): the generic
     plane and split engines with their tile widths, z rows per block and
@@ -121,7 +122,8 @@ def candidates(dims):
         tiles = [w for w in (8, 16, 32) if n0 * w <= 8192]
         for b in (64, 32, 16):
             for w in tiles:
-                yield dict(variant=3, batch=b, tile_w=w)
+                for o in (0, 1):
+                    yield dict(variant=3, batch=b, tile_w=w, options=o)
     if all(_smooth(n) for n in dims):
         fused = True
         for b in (8, 4, 16, 32):
@@ -174,9 +176,11 @@ def time_config(dims, n_atoms, tuning, frames=64, reps=3, device=None, positions
     return e0.elapsed_time(e1) / (reps * p4.shape[0])
 
 
-def tune(dims, n_atoms=200_000, max_candidates=None, frames=64, device=None, verbose=False):
-    """Time the candidates of `dims` (at most `max_candidates`), store the
-    fastest in the cache and return it."""
+def tune(dims, n_atoms=200_000, max_candidates=None, frames=128, device=None, verbose=False):
+    """Time the candidates of `dims` (at most `max_candidates`) on `frames`
+    frames, store the fastest in the cache and return it.  The default of
+    128 frames spans several batches, so the overlap of one batch's x pass
+    with the next batch's plane FFT is part of what is timed."""
     import torch
     from . import plan as _plan
     dims = tuple(int(d) for d in dims)
@@ -214,7 +218,7 @@ def tune(dims, n_atoms=200_000, max_candidates=None, frames=64, device=None, ver
     return dict(best)
 
 
-def tune_for(dims, n_atoms=200_000, max_candidates=None, frames=64, device=None):
+def tune_for(dims, n_atoms=200_000, max_candidates=None, frames=128, device=None):
     """The cached tuning of `dims` on this GPU, tuning the shape first if the
     cache has no entry for it."""
     t = lookup(dims)
