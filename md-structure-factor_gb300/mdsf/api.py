@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import tune as _tune
-from ._lib import MSF_WRAP, c_p, call
+from ._lib import MSF_CONTINUE, MSF_WRAP, c_p, call
 from .plan import get_plan, stream_ptr
 
 
@@ -81,6 +81,20 @@ def _side_stream(device):
 
 
 _CHAIN = {4: "msf_hist_sf_f32", 3: "msf_hist_sf_f32xyz", 8: "msf_hist_sf_f64"}
+
+
+def _chunk_sizes(T, chunk, lead=True):
+    """Frames per host-to-device chunk: `chunk` each, or (lead) a first
+    chunk of a quarter of it -- its copy is the one no kernel hides -- and
+    the rest in near-equal chunks of at most `chunk` frames.  For 100 frames
+    in chunks of 64 that is 16 + 42 + 42: 25.0 against 25.9 us per frame for
+    64 + 36 on the GB300, copies and kernels together."""
+    if not lead or T <= chunk:
+        return [min(chunk, T - f) for f in range(0, T, chunk)]
+    first = max(1, chunk // 4)
+    rest = T - first
+    n = -(-rest // chunk)
+    return [first] + [rest // n + (1 if i < rest % n else 0) for i in range(n)]
 
 
 def _launch_chain(plan, code, p, w, N, T, sc, flags, sf, st):
@@ -185,13 +199,14 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
                 hp = hp.contiguous().pin_memory()
             main = torch.cuda.current_stream(device)
             side = _side_stream(device)
-            bufs = [torch.empty((chunk, N, C), dtype=tdt, device=device) for _ in range(2)]
+            sizes = _chunk_sizes(T, chunk, lead=stream_chunk is None)
+            bufs = [torch.empty((max(sizes), N, C), dtype=tdt, device=device) for _ in range(2)]
             copied = [torch.cuda.Event() for _ in range(2)]
             free = [None, None]
             for b in bufs:
                 b.record_stream(side)
-            for i, f0 in enumerate(range(0, T, chunk)):
-                k = min(chunk, T - f0)
+            f0 = 0
+            for i, k in enumerate(sizes):
                 b = i % 2
                 with torch.cuda.stream(side):
                     if free[b] is not None:
@@ -199,11 +214,15 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
                     bufs[b][:k].copy_(hp[f0:f0 + k], non_blocking=True)
                     copied[b].record(side)
                 main.wait_event(copied[b])
+                # one chain over the chunks: a bucketed plan's x pass of one
+                # chunk then overlaps the plane FFT of the next
+                more = MSF_CONTINUE if i + 1 < len(sizes) else 0
                 _launch_chain(plan, code, bufs[b].data_ptr(), wptr, N, k,
-                              scp + 24 * f0 if scp else 0, flags, sf, st)
+                              scp + 24 * f0 if scp else 0, flags | more, sf, st)
                 ev = torch.cuda.Event()
                 ev.record(main)
                 free[b] = ev
+                f0 += k
     if mean and T > 0:
         sf.div_(T)
     return sf

@@ -83,3 +83,16 @@ def test_candidates_cover_the_fused_and_generic_chains():
     assert {c["variant"] for c in _tune.candidates((256, 256, 128))} == {3, 4}
     assert {c["variant"] for c in _tune.candidates((75, 48, 81))} == {4}
     assert {c["variant"] for c in _tune.candidates((74, 64, 26))} <= {1, 2}
+
+
+def test_host_chunks_lead_short_then_balanced():
+    from mdsf.api import _chunk_sizes
+    assert _chunk_sizes(100, 64) == [16, 42, 42]
+    assert _chunk_sizes(64, 64) == [64]
+    assert _chunk_sizes(100, 64, lead=False) == [64, 36]
+    for T in range(1, 300, 7):
+        for c in (1, 4, 16, 50, 64):
+            z = _chunk_sizes(T, c)
+            assert sum(z) == T and max(z) <= c and min(z) >= 1
+            if T > c:
+                assert z[0] == max(1, c // 4) and max(z[1:]) - min(z[1:]) <= 1
