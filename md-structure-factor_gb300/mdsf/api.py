@@ -199,7 +199,8 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
                 hp = hp.contiguous().pin_memory()
             main = torch.cuda.current_stream(device)
             side = _side_stream(device)
-            sizes = _chunk_sizes(T, chunk, lead=stream_chunk is None)
+            # the short lead chunk pays only where the chunk calls overlap (bucketed plans)
+            sizes = _chunk_sizes(T, chunk, lead=stream_chunk is None and plan.variant == 3)
             bufs = [torch.empty((max(sizes), N, C), dtype=tdt, device=device) for _ in range(2)]
             copied = [torch.cuda.Event() for _ in range(2)]
             free = [None, None]
