@@ -56,8 +56,10 @@ struct BucketArgs {
 constexpr int kBucketThreads = 256;
 constexpr int kBucketIter = kBucketAtoms / kBucketThreads;
 
+// five blocks per SM (48 registers; 58 without the bound): the sort is bound
+// by the latency of its position loads, so resident warps are what it needs
 template <int MODE>
-__global__ void __launch_bounds__(kBucketThreads) k_bucket_sort(BucketArgs a) {
+__global__ void __launch_bounds__(kBucketThreads, 5) k_bucket_sort(BucketArgs a) {
   constexpr bool kTab = MODE == 0 || MODE == 3;   // FP32 search: edge tables in shared memory
   __shared__ int hist[kMaxN + 1];
   __shared__ int warp_sum[kBucketThreads / 32];
