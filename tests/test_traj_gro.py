@@ -10,14 +10,15 @@ import pytest
 from mdsf import traj
 from oracle import gro as ogro
 
-# the reference's own test data (read in place when the checkout is present)
-REF_TEST = "/root/reference/test"
+# the reference's own test data, read in place from the checkout named by
+# MSF_REFERENCE (its test/ directory); skipped when that is not set
+REF_ROOT = os.environ.get("MSF_REFERENCE", "")
 
 
 def ref_file(name):
-    p = os.path.join(REF_TEST, name)
-    if not os.path.isfile(p):
-        pytest.skip("reference checkout not present")
+    p = os.path.join(REF_ROOT, "test", name)
+    if not REF_ROOT or not os.path.isfile(p):
+        pytest.skip("reference checkout not given (MSF_REFERENCE)")
     return p
 
 
