@@ -8,36 +8,33 @@ namespace msf {
 //   k >= nh-2 : sf[(i+1+n0/2) % n0, (j+1+n1/2) % n1, k-nh+2]        (shifted copy)
 //   k <  nh-2 : sf[(n0-1-i+n0/2) % n0, (n1-1-j+n1/2) % n1, nh-2-k]   (z mirror)
 // and the DC voxel (n0/2-1, n1/2-1, nh-2) := 1/3*((sf[1,0,0] + sf[0,1,0]) + sf[0,0,1]).
+// One CTA per output line (i, j) at a time, its threads along k: the index
+// arithmetic is one 32-bit division per line instead of 64-bit divisions
+// per voxel, and both the reads of a line (ascending or, mirrored,
+// descending z) and its writes stay contiguous.
 __global__ void k_sfplt(const double* __restrict__ sf, int n0, int n1, int nh,
                         double* __restrict__ out) {
   const int m0 = n0 - 2, m1 = n1 - 2, m2 = 2 * nh - 3;
-  const int64_t total = (int64_t)m0 * m1 * m2;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % m2);
-    const int64_t r = e / m2;
-    const int j = (int)(r % m1);
-    const int i = (int)(r / m1);
-    int sx, sy, sz;
-    if (k >= nh - 2) {
-      sx = (i + 1 + n0 / 2) % n0;
-      sy = (j + 1 + n1 / 2) % n1;
-      sz = k - nh + 2;
-    } else {
-      sx = (n0 - 1 - i + n0 / 2) % n0;
-      sy = (n1 - 1 - j + n1 / 2) % n1;
-      sz = nh - 2 - k;
+  const int lines = m0 * m1;
+  for (int line = blockIdx.x; line < lines; line += gridDim.x) {
+    const int i = line / m1, j = line - i * m1;
+    // source rows of the shifted copy (k >= nh-2) and of the z mirror
+    const int64_t up = ((int64_t)((i + 1 + n0 / 2) % n0) * n1 + (j + 1 + n1 / 2) % n1) * nh;
+    const int64_t dn = ((int64_t)((n0 - 1 - i + n0 / 2) % n0) * n1 + (n1 - 1 - j + n1 / 2) % n1) * nh;
+    const bool dc_line = i == n0 / 2 - 1 && j == n1 / 2 - 1;
+    double* o = out + (int64_t)line * m2;
+    for (int k = threadIdx.x; k < m2; k += blockDim.x) {
+      double v;
+      if (dc_line && k == nh - 2) {
+        const double a = __ldg(sf + (int64_t)1 * n1 * nh);
+        const double b = __ldg(sf + nh);
+        const double c = __ldg(sf + 1);
+        v = __dmul_rn(1.0 / 3.0, __dadd_rn(__dadd_rn(a, b), c));
+      } else {
+        v = k >= nh - 2 ? __ldg(sf + up + (k - nh + 2)) : __ldg(sf + dn + (nh - 2 - k));
+      }
+      o[k] = v;
     }
-    double v;
-    if (i == n0 / 2 - 1 && j == n1 / 2 - 1 && k == nh - 2) {
-      const double a = __ldg(sf + (int64_t)1 * n1 * nh);
-      const double b = __ldg(sf + nh);
-      const double c = __ldg(sf + 1);
-      v = __dmul_rn(1.0 / 3.0, __dadd_rn(__dadd_rn(a, b), c));
-    } else {
-      v = __ldg(sf + ((int64_t)sx * n1 + sy) * nh + sz);
-    }
-    out[e] = v;
   }
 }
 
@@ -47,10 +44,12 @@ __device__ __forceinline__ int find_interval(const double* __restrict__ x, int n
   const double a = __ldg(x), b = __ldg(x + n - 1);
   if (!(a <= v && v <= b)) return -1;
   if (v == b) return n - 2;
-  const double h = __ddiv_rn(__dsub_rn(b, a), (double)(n - 1));
-  // first guess, clamped before the conversion (NaN -> 0), then corrected
-  const double g = (v - a) / h;
-  int i = g >= (double)(n - 2) ? n - 2 : (g >= 0.0 ? (int)g : 0);
+  // first guess for an evenly spaced axis, in FP32 (an FP64 division costs
+  // more than the correction steps it saves), clamped before the conversion
+  // (NaN -> 0), then corrected exactly: any start in [0, n-2] ends at the
+  // same interval
+  const float g = (float)(v - a) * ((float)(n - 1) / (float)(b - a));
+  int i = g >= (float)(n - 2) ? n - 2 : (g >= 0.f ? (int)g : 0);
   while (i > 0 && v < __ldg(x + i)) --i;
   while (i < n - 2 && v >= __ldg(x + i + 1)) ++i;
   return i;
@@ -402,9 +401,10 @@ int msf_sfplt(const double* sf, int32_t n0, int32_t n1, int32_t nh, double* out,
               msf_stream_t stream) {
   if (!sf || !out) return MSF_E_INVALID;
   if (n0 < 4 || n1 < 4 || nh < 3 || (n0 & 1) || (n1 & 1)) return MSF_E_UNSUPPORTED;
-  const int64_t total = (int64_t)(n0 - 2) * (n1 - 2) * (2 * nh - 3);
-  const int blocks = (int)((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
-  k_sfplt<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(sf, n0, n1, nh, out);
+  const int lines = (n0 - 2) * (n1 - 2);
+  const int threads = 2 * nh - 3 <= 128 ? 128 : 256;
+  const int blocks = lines < 152 * 16 ? lines : 152 * 16;
+  k_sfplt<<<blocks, threads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(sf, n0, n1, nh, out);
   return launch_status();
 }
 
