@@ -361,7 +361,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-errors", action="store_true", help="skip the per-configuration oracle errors")
     ap.add_argument("--stream-chunk", type=int, default=0,
-                    help="frames per host->device chunk of the e2e path (0: the API default, one batch)")
+                    help="frames per host->device chunk of the e2e path (0: the API default: a quarter-batch lead chunk, then near-equal chunks of at most one batch)")
     ap.add_argument("--stress-only", action="store_true",
                     help="only the 512^3 stress grid (1M atoms, 200 frames from pinned host memory)")
     ap.add_argument("--stress-frames", type=int, default=200)
