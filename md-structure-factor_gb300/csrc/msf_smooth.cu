@@ -45,8 +45,14 @@ __device__ __forceinline__ float load_any(const void* g, int kind, int64_t i) {
   return load_grid<kGridF64>(g, i);
 }
 
+// three CTAs per SM (80 registers) for the 512-point lines, which used 94
+// registers (two CTAs per SM) on their own: the 512^3 stress grid went from
+// 562 to 600-700 frames/s.  The other lengths keep the compiler's choice
+// (the same bound on the 256-point lines cost the batched systems 4%)
+__host__ __device__ constexpr int zs_min_blocks(int n2) { return n2 == 512 ? 3 : 1; }
+
 template <int N2>
-__global__ void __launch_bounds__(kSmoothThreads) k_zs(SmZArgs a) {
+__global__ void __launch_bounds__(kSmoothThreads, zs_min_blocks(N2)) k_zs(SmZArgs a) {
   constexpr int G = smooth_rows(N2), S = G + 1, NH = N2 / 2 + 1, NT = kSmoothThreads;
   extern __shared__ __align__(16) float2 smem[];
   float2* buf = smem;              // [N2][S]: sample z of line g at buf[z*S + g]
