@@ -7,12 +7,12 @@
 // an mbarrier, so the copies of items s+1 .. s+NS-1 run while item s is
 // transformed (NS = 2: four buffers per 16 KB tile measured slower alone, as
 // they cost half the CTAs per SM).  Tiles of at most 2048 values take
-// 128-thread CTAs: beside a plane-FFT CTA (the overlapped launch) two of them
-// fit, alone six per SM.  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed
-// over the frames of the tile in FP32, one FP64 read-modify-write of sf per
-// tile every kPowerFlush frames and after the last.  Waits are bounded: on
-// timeout the kernel latches MSF_E_TIMEOUT in the plan status word and
-// returns.
+// 128-thread CTAs: beside a plane-FFT CTA (the overlapped launch) two of
+// them fit, alone six per SM.  x-FFT (DIF, natural input, output at pos(k)),
+// |F|^2 summed over the frames of the tile in FP32, one FP64
+// read-modify-write of sf per tile every kPowerFlush frames and after the
+// last.  Waits are bounded: on timeout the kernel latches MSF_E_TIMEOUT in
+// the plan status word and returns.
 #include "msf_ct.cuh"
 #include "msf_r2.cuh"
 #include "msf_tma.cuh"
