@@ -83,6 +83,25 @@ def test_bucketed_headline_grid_batches(batch):
     assert e < TOL
 
 
+@pytest.fixture(scope="module")
+def headline_five_frames():
+    pos, box, w = synth.columnar(frames=5, seed=4)
+    return pos, box, w, ohist.hist_sf(pos, box, w, (256, 256, 128))
+
+
+@pytest.mark.parametrize("tile_w", [8, 16, 32])
+@pytest.mark.parametrize("options", [0, 1])
+def test_headline_grid_x_tiles_and_overlap(headline_five_frames, tile_w, options):
+    """Batches of 2 over 5 frames: with the overlap (options 0) the x passes
+    of the first two batches run beside the next plane FFT (8-column tiles on
+    two 128-thread CTAs per SM, 16- and 32-column ones on 256-thread CTAs) and
+    the last alone; the plane kernel hands its planes out by its counter."""
+    pos, box, w, ref = headline_five_frames
+    got = mdsf.structure_factor(synth.pack_float4(pos, w), box, None, (256, 256, 128),
+                                tuning=dict(variant=3, batch=2, tile_w=tile_w, options=options)).cpu().numpy()
+    assert np.abs(got - ref).max() / ref.max() < TOL
+
+
 def test_power_accum_ct_grids():
     rng = np.random.default_rng(3)
     for dims in [(64, 64, 64), (256, 128, 64), (32, 128, 256)]:
