@@ -298,10 +298,9 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
     if (s) return s;
   }
   if (p->overlap && !p->side) {
-    // two streams of equal (default) priority: with the main-stream work on
-    // the caller's stream, a legacy default or a high-priority caller stream
-    // left the x passes waiting behind the plane FFTs (640 frames measured
-    // 30.5 against 23.2 us per frame on a plain stream)
+    // two streams of equal (default) priority, whatever the caller's stream
+    // is (a legacy default stream, or one of raised priority that would give
+    // the plane FFTs precedence over the x passes)
     if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
     if (cudaStreamCreateWithFlags(&p->plane_st, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
     for (int i = 0; i < 2; ++i) {
