@@ -688,7 +688,7 @@ def config_errors(torch, dev, sf_timed, pos, box, w, direct_S=None):
             a["max"], a["rms"] = max(a["max"], e["max"]), max(a["rms"], e["rms"])
         out.update(agg)
         out["config1"]["sample"] = "the whole workload (10 frames)"
-        out["config2"]["sample"] = "the sf of the timed step (100 frames, 64-frame batches)"
+        out["config2"]["sample"] = "the sf of the timed step (100 frames, two 50-frame batches)"
         out["config3"]["sample"] = (f"{len(pick)} of the 64 systems (incl. the most atoms and the largest grid), "
                                     "2 frames each, one graph; worst system")
         out["config5"]["sample"] = "2 frames of the 1M-atom system on 512^3"

@@ -147,8 +147,10 @@ int msf_power_accum_f32(msf_plan* plan, const float* grids, int32_t n_grids, dou
 /* ------------------------------------------ fused chain (a2, a4, a5, a8, a9)
  * For frames t in [0, n_frames): deposit frame t's histogram, rfftn,
  * |F|^2 and sf += -- the whole per-frame loop of dens.py:277-321 in
- * histogram form, batched `batch` frames per pass.  sf is accumulated
- * (the reference's undivided sum, dens.py:318).
+ * histogram form, batched at most `batch` frames per pass (a bucketed plan
+ * with the overlap splits a call into ceil(n_frames / batch) near-equal
+ * batches).  sf is accumulated (the reference's undivided sum,
+ * dens.py:318).
  *   pos_w:  (n_frames, n_atoms) float4 (x, y, z, w).
  *   scale:  NULL or (n_frames, 3) doubles (per-frame rescale factors).
  * Input arrays (positions, weights, scale) of the deposit and chain calls

@@ -181,8 +181,14 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
     const cudaStream_t caller = st;
     st = p->plane_st;
     int64_t k = p->chain_k;
-    for (int64_t f = 0; f < n_frames && !s; f += p->batch, ++k) {
-      const int nb = (int)((n_frames - f < p->batch) ? n_frames - f : p->batch);
+    // near-equal batches of at most p->batch frames: after a full batch a
+    // short last one left the full batch's x pass to run on at one CTA per SM
+    // once the short plane FFT beside it had ended (100 frames as 64 + 36:
+    // 26.3 us per frame eager, 23.5 as 50 + 50; 160 frames as 64 + 64 + 32 in
+    // a graph: 24.9 against 23.0 as 54 + 53 + 53)
+    const int64_t nbat = (n_frames + p->batch - 1) / p->batch;
+    for (int64_t f = 0, i = 0; f < n_frames && !s; ++i, ++k) {
+      const int nb = (int)(n_frames / nbat + (i < n_frames % nbat ? 1 : 0));
       const int buf = (int)(k & 1);
       const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;
       s = fused_bucket_batch(p, fp, weights, layout, n_atoms, nb, fstride, scale ? scale + 3 * f : nullptr,
@@ -194,6 +200,7 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
       // the last x pass of a chain has the SMs to itself
       if (!s) s = fused_x_batch(p, nb, sf, p->side, buf, !cont && f + nb >= n_frames);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_x[buf], p->side));
+      f += nb;
     }
     if (!s) s = cuda_status(cudaEventRecord(p->ev_plane_st, st));
     if (!s) s = cuda_status(cudaStreamWaitEvent(caller, p->ev_plane_st, 0));

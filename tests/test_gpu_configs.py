@@ -85,8 +85,9 @@ def test_config1_water_box(oracle_pool):
 def test_config2_benchmarked_chain(oracle_pool):
     """The benchmarked step exactly: the columnar system (200,000 atoms,
     16.0 x 13.856 x 8.0 nm, seed 2), 100 float32 frames, 256 x 256 x 128, on
-    the default plan (bucketed chain, 64-frame batches, x pass overlapped on
-    the plan's side stream) called through the C ABI, then get_dplot and the
+    the default plan (bucketed chain, batches of at most 64 frames -- two of
+    50 here --, x pass overlapped on the plan's side stream) called through
+    the C ABI, then get_dplot and the
     Ewald slices at lambda = 0.154 nm."""
     dims, n, T = (256, 256, 128), 200_000, 100
     pos, box, w = synth.columnar(n_atoms=n, frames=T, seed=2)
@@ -100,7 +101,7 @@ def test_config2_benchmarked_chain(oracle_pool):
     ref, = pool_hist_sf(oracle_pool, [(pos, box, w, dims)])
     got = sf.cpu().numpy()
     e, rms = errors(got, ref)
-    print(f"config 2 (columnar 200k atoms, 256x256x128, 100 frames, 64-frame batches): "
+    print(f"config 2 (columnar 200k atoms, 256x256x128, 100 frames, two 50-frame batches): "
           f"max err {e:.2e}, rms {rms:.2e} of max(S)")
     assert e < TOL
     check_post(sf, box)

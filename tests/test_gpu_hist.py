@@ -196,8 +196,8 @@ def test_full_workload_properties():
     hold at any size against exact integer references: the DC term is the
     squared electron count of each frame (no atom lost or doubled), Parseval
     over the full spectrum equals V * sum of the exact int32 grid squared,
-    S is finite and non-negative, and two calls split at the batch boundary
-    add up to one call bit for bit."""
+    S is finite and non-negative, and two calls split at the boundary of the
+    chain's first (near-equal) batch add up to one call bit for bit."""
     pos, box, w = synth.columnar(frames=100, seed=2)
     p4 = torch.from_numpy(synth.pack_float4(pos, w)).cuda()
     dims = (256, 256, 128)
@@ -218,9 +218,11 @@ def test_full_workload_properties():
     assert abs(full - V * float(sumsq)) <= 1e-5 * V * float(sumsq)
     assert np.all(np.isfinite(s)) and s.min() >= 0.0
     batch = mdsf.get_plan(dims, box, max_atoms=p4.shape[1]).batch
-    assert batch < p4.shape[0]
-    a = mdsf.structure_factor(p4[:batch], box, None, dims)
-    b = mdsf.structure_factor(p4[batch:], box, None, dims)
+    T = p4.shape[0]
+    assert batch < T
+    first = -(-T // -(-T // batch))   # the chain's near-equal batches: the first one's end
+    a = mdsf.structure_factor(p4[:first], box, None, dims)
+    b = mdsf.structure_factor(p4[first:], box, None, dims)
     assert torch.equal(a + b, sf)
 
 
