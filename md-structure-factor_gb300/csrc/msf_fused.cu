@@ -761,16 +761,29 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_compact(BucketArgs a,
     sdst[i] = cnt ? atomicAdd(cursor + (int64_t)frame * n0 + i, cnt) : 0;
   }
   __syncthreads();
-  const int total = sbo[n0];
   const int2* src = a.bucket + ((int64_t)frame * a.nblk + blk) * kBucketAtoms;
   int2* out = pbucket + (int64_t)frame * pstride;
-  for (int e = threadIdx.x; e < total; e += kBucketThreads) {
-    int lo = 0, hi = n0 - 1;
-    while (lo < hi) {
-      const int m = (lo + hi + 1) >> 1;
-      if (sbo[m] <= e) lo = m; else hi = m - 1;
+  // warp w moves the entries of planes 32w .. 32w+31 (then w + 8, ...):
+  // lane l holds plane 32w+l's segment start and destination, and an entry
+  // finds its plane -- the last lane whose start is <= it -- by a 5-step
+  // search over the lanes' registers (the starts ascend with the lane)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int p0 = warp * 32; p0 < n0; p0 += kBucketThreads) {
+    const int pl = p0 + lane;
+    const int start = pl < n0 ? sbo[pl] : sbo[n0];
+    const int dst = pl < n0 ? sdst[pl] : 0;
+    const int beg = sbo[p0], end = sbo[min(p0 + 32, n0)];
+    for (int base = beg; base < end; base += 32) {
+      const int e = base + lane;
+      int lo = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int probe = __shfl_sync(0xffffffffu, start, lo + step);
+        if (probe <= e) lo += step;
+      }
+      const int s0 = __shfl_sync(0xffffffffu, start, lo), d0 = __shfl_sync(0xffffffffu, dst, lo);
+      if (e < end) out[d0 + (e - s0)] = src[e];
     }
-    out[sdst[lo] + (e - sbo[lo])] = src[e];
   }
 }
 
