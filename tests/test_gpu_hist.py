@@ -190,6 +190,29 @@ def test_continue_flag_equals_one_call():
     assert rel_err(one.cpu().numpy(), ref) < TOL
 
 
+@pytest.mark.parametrize("priority", [0, -1])
+def test_overlapped_chain_on_a_caller_stream(priority):
+    """The overlapped chain forks its two plan-owned streams from the
+    caller's stream and joins them back: called on a non-default stream (of
+    default or raised priority), the sf is complete on that stream when the
+    call returns, across MSF_CONTINUE calls too, and equals the oracle's."""
+    from mdsf._lib import MSF_CONTINUE, c_p, call
+    pos, box, w = synth.uniform_system(4000, (2.0, 2.0, 2.0), frames=7, seed=8)
+    p4 = torch.from_numpy(synth.pack_float4(pos.astype(np.float32), w)).cuda()
+    plan = mdsf.get_plan((64, 64, 64), box, max_atoms=4000, batch=2, variant=3)
+    s = torch.cuda.Stream(priority=priority)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        st = c_p(s.cuda_stream)
+        sf = torch.zeros(plan.half_shape, dtype=torch.float64, device="cuda")
+        for f0, f1, fl in ((0, 3, MSF_CONTINUE), (3, 7, 0)):
+            call("msf_hist_sf_f32", plan.handle, c_p(p4[f0:f1].data_ptr()), 4000, f1 - f0, c_p(0), fl,
+                 c_p(sf.data_ptr()), st)
+        host = sf.to("cpu", non_blocking=False)   # ordered on s only
+    ref = ohist.hist_sf(pos.astype(np.float32), box, w, (64, 64, 64))
+    assert rel_err(host.numpy(), ref) < TOL
+
+
 def test_full_workload_properties():
     """The headline workload itself (columnar 200k atoms, 100 frames,
     256x256x128, the plan's default batch), checked through properties that
