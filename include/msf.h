@@ -86,13 +86,14 @@ typedef struct msf_plan_desc {
 } msf_plan_desc;
 
 /* msf_plan_desc.options.  By default a variant-3 plan double-buffers its
- * spectra and msf_plan_bind creates two internal streams of default
- * priority and six events: a call over more than one batch runs the bucket
- * sort and plane FFT of each batch on one of them and the batch's x pass on
- * the other, overlapped with the plane FFT of the next batch (forked from
- * and joined back to the caller's stream, so the calls stay stream-ordered
- * and graph-capturable; the caller's stream has passed the positions when
- * the call's work on it completes, with or without MSF_CONTINUE).
+ * spectra and its bucket arrays, and msf_plan_bind creates three internal
+ * streams (the plane FFTs' at the device's greatest priority, the others at
+ * the default) and eight events: a call over more than one batch runs each
+ * batch's bucket sort beside the previous batch's plane FFT, its plane FFT,
+ * and its x pass beside the next batch's plane FFT (forked from and joined
+ * back to the caller's stream, so the calls stay stream-ordered and
+ * graph-capturable; the caller's stream has passed the positions when the
+ * call's work on it completes, with or without MSF_CONTINUE).
  * The kernels' waits on their own asynchronous copies are bounded (2^26
  * polls of the mbarrier): a wait that runs out latches MSF_E_TIMEOUT, the
  * kernel returns, and msf_plan_status() reports it.  MSF_PLAN_DIAG_STALL is

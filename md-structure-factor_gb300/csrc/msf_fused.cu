@@ -787,21 +787,24 @@ __global__ void __launch_bounds__(kBucketThreads) k_bucket_compact(BucketArgs a,
   }
 }
 
-static BucketArgs bucket_args(const msf_plan* p) {
+static BucketArgs bucket_args(const msf_plan* p, int slot = 0) {
+  const size_t d = slot ? p->bk_delta : 0;
   BucketArgs b;
   b.d = dep_args(p);
-  b.boff = ws_ptr<int>(p, p->off_offsets);
-  b.bucket = ws_ptr<int2>(p, p->off_bucket);
+  b.boff = ws_ptr<int>(p, p->off_offsets + d);
+  b.bucket = ws_ptr<int2>(p, p->off_bucket + d);
   b.nblk = (int)((p->max_atoms + kBucketAtoms - 1) / kBucketAtoms);
-  b.pcount = ws_ptr<int>(p, p->off_pcount);
+  b.pcount = ws_ptr<int>(p, p->off_pcount + d);
   return b;
 }
 
 int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
                        int64_t n_atoms, int nframes, int64_t frame_stride, const double* scale,
-                       int flags, cudaStream_t st) {
+                       int flags, cudaStream_t st, int slot) {
   if (n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
-  BucketArgs b = bucket_args(p);
+  if (slot && !p->bk_delta) return MSF_E_INVALID;
+  const size_t d = slot ? p->bk_delta : 0;
+  BucketArgs b = bucket_args(p, slot);
   b.d.pos = pos;
   b.d.w = weights;
   b.d.n_atoms = n_atoms;
@@ -821,9 +824,9 @@ int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weight
   }
   int s = launch_status();
   if (s) return s;
-  int2* pbucket = ws_ptr<int2>(p, p->off_pbucket);
-  int* cursor = ws_ptr<int>(p, p->off_pcursor);
-  k_bucket_scan<<<nframes, ((p->n0 + 31) / 32) * 32, 0, st>>>(b.pcount, p->n0, ws_ptr<int>(p, p->off_poff), cursor,
+  int2* pbucket = ws_ptr<int2>(p, p->off_pbucket + d);
+  int* cursor = ws_ptr<int>(p, p->off_pcursor + d);
+  k_bucket_scan<<<nframes, ((p->n0 + 31) / 32) * 32, 0, st>>>(b.pcount, p->n0, ws_ptr<int>(p, p->off_poff + d), cursor,
                                                           pbucket, p->pstride);
   s = launch_status();
   if (s) return s;
@@ -857,7 +860,8 @@ int bucket_grid(const msf_plan* p, const void* pos, const int32_t* weights, int 
   return launch_status();
 }
 
-static PlaneCtArgs plane_args(const msf_plan* p) {
+static PlaneCtArgs plane_args(const msf_plan* p, int slot = 0) {
+  const size_t d = slot ? p->bk_delta : 0;
   PlaneCtArgs a;
   memset(&a, 0, sizeof(a));
   a.n0 = p->n0;
@@ -865,8 +869,8 @@ static PlaneCtArgs plane_args(const msf_plan* p) {
   a.C = ws_ptr<float2>(p, p->off_cplx);
   a.Vh = half_elems(p);
   a.twy = ws_ptr<float2>(p, p->off_tw[1]);
-  a.pbucket = ws_ptr<int2>(p, p->off_pbucket);
-  a.poff = ws_ptr<int>(p, p->off_poff);
+  a.pbucket = ws_ptr<int2>(p, p->off_pbucket + d);
+  a.poff = ws_ptr<int>(p, p->off_poff + d);
   a.pstride = p->pstride;
   a.status = ws_ptr<int>(p, p->off_status);
   a.next_item = ws_ptr<int>(p, p->off_pnext);
@@ -876,8 +880,9 @@ static PlaneCtArgs plane_args(const msf_plan* p) {
 }
 
 int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st,
-                      int buf) {
-  PlaneCtArgs a = plane_args(p);
+                      int buf, int slot) {
+  if (slot && !p->bk_delta) return MSF_E_INVALID;
+  PlaneCtArgs a = plane_args(p, slot);
   if (buf) a.C = ws_ptr<float2>(p, p->off_cplx2);
   a.grids = grids;
   a.grid_kind = grid_kind;

@@ -167,16 +167,20 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
                        : (layout == kLayoutF64 ? sizeof(double) : sizeof(float));
   if (p->variant == 3 && n_atoms > p->max_atoms) return MSF_E_WORKSPACE;
   if (p->variant == 3 && p->overlap && (n_frames > p->batch || cont || p->chain_k > 0)) {
-    // batch b: bucket sort + plane FFT into spectrum buffer b%2 on `plane_st`,
-    // the x pass of batch b on `side` (after that plane FFT), overlapping the
-    // plane FFT of batch b+1; the plane FFT of batch b+2 waits for the x pass
-    // of batch b before reusing its buffer.  `plane_st` starts after the
-    // caller's prior work and the caller's stream waits for it at the
-    // end of every call (the positions have been read); it joins `side` at
-    // the end of the chain.  With MSF_CONTINUE the batch count carries over
+    // batch b: bucket sort into bucket slot b%2 on `bucket_st` (beside the
+    // plane FFT of batch b-1), plane FFT into spectrum buffer b%2 on
+    // `plane_st` (after that bucket sort), the x pass of batch b on `side`
+    // (after that plane FFT), overlapping the plane FFT of batch b+1; the
+    // bucket sort and plane FFT of batch b+2 wait for the plane FFT and the x
+    // pass of batch b before reusing its slot and buffer.  The plan's streams
+    // start after the caller's prior work and the caller's stream waits for
+    // `plane_st` -- and through it every bucket sort: the positions have been
+    // read -- at the end of every call; it joins `side` at the end of the
+    // chain.  With MSF_CONTINUE the batch count carries over
     // to the next call and that join is left to the call that ends the
     // chain.
     int s = cuda_status(cudaEventRecord(p->ev_fork, st));
+    if (!s) s = cuda_status(cudaStreamWaitEvent(p->bucket_st, p->ev_fork, 0));
     if (!s) s = cuda_status(cudaStreamWaitEvent(p->plane_st, p->ev_fork, 0));
     const cudaStream_t caller = st;
     st = p->plane_st;
@@ -189,12 +193,19 @@ static int hist_sf_any(msf_plan* p, const void* pos, const int32_t* weights, int
     const int64_t nbat = (n_frames + p->batch - 1) / p->batch;
     for (int64_t f = 0, i = 0; f < n_frames && !s; ++i, ++k) {
       const int nb = (int)(n_frames / nbat + (i < n_frames % nbat ? 1 : 0));
-      const int buf = (int)(k & 1);
+      const int buf = (int)(k & 1);   // spectrum buffer and bucket slot
       const void* fp = static_cast<const char*>(pos) + (size_t)f * fstride * esize;
-      s = fused_bucket_batch(p, fp, weights, layout, n_atoms, nb, fstride, scale ? scale + 3 * f : nullptr,
-                             flags, st);
+      // the bucket sort of batch k on its own stream, into slot buf once the
+      // plane FFT of batch k-2 has read that slot: it runs beside the plane
+      // FFT of batch k-1
+      if (!s && k >= 2) s = cuda_status(cudaStreamWaitEvent(p->bucket_st, p->ev_plane[buf], 0));
+      if (!s)
+        s = fused_bucket_batch(p, fp, weights, layout, n_atoms, nb, fstride, scale ? scale + 3 * f : nullptr,
+                               flags, p->bucket_st, buf);
+      if (!s) s = cuda_status(cudaEventRecord(p->ev_bucket[buf], p->bucket_st));
+      if (!s) s = cuda_status(cudaStreamWaitEvent(st, p->ev_bucket[buf], 0));
       if (!s && k >= 2) s = cuda_status(cudaStreamWaitEvent(st, p->ev_x[buf], 0));
-      if (!s) s = fused_plane_batch(p, nullptr, kGridI32, nb, st, buf);
+      if (!s) s = fused_plane_batch(p, nullptr, kGridI32, nb, st, buf, buf);
       if (!s) s = cuda_status(cudaEventRecord(p->ev_plane[buf], st));
       if (!s) s = cuda_status(cudaStreamWaitEvent(p->side, p->ev_plane[buf], 0));
       // the last x pass of a chain has the SMs to itself

@@ -69,6 +69,9 @@ struct msf_plan {
   // even count), the plane offsets, the per-plane counts (kept zero between
   // batches) and the per-plane placement cursors
   size_t off_pbucket, off_poff, off_pcount, off_pcursor, off_pnext;
+  // bytes from the first copy of the bucket arrays (off_offsets ..
+  // off_pcursor's end) to the second (overlap only; 0 otherwise)
+  size_t bk_delta;
   int64_t pstride;      // entries per frame in the compacted array
   // TMA tensor maps over the two spectrum buffers for the x pass (CUtensorMap, 128 bytes each)
   alignas(64) unsigned char xtma_map[2][128];
@@ -80,8 +83,8 @@ struct msf_plan {
   // (ev_plane_st, ev_x).  Created by msf_plan_bind, released by plan_release
   int overlap;
   size_t off_cplx2;
-  cudaStream_t side, plane_st;
-  cudaEvent_t ev_plane[2], ev_x[2], ev_fork, ev_plane_st;
+  cudaStream_t side, plane_st, bucket_st;
+  cudaEvent_t ev_plane[2], ev_x[2], ev_fork, ev_plane_st, ev_bucket[2];
   // a chain continued over several calls (MSF_CONTINUE): batches issued so
   // far, for the spectrum-buffer parity and the reuse waits; 0 when joined
   int64_t chain_k;
@@ -332,11 +335,13 @@ int hist_sf_chain(msf_plan* p, const void* pos, const int32_t* weights, int layo
 bool ct_plane_ok(int n1, int n2);
 int ct_x_width(int n0, int requested);   // 0 when no x kernel exists for n0 (and width)
 size_t ct_plane_smem(int n1, int n2);
+// slot: which copy of the bucket arrays (two with the overlap, so that the
+// bucket sort of batch b+1 runs beside the plane FFT of batch b)
 int fused_bucket_batch(const msf_plan* p, const void* pos, const int32_t* weights, int layout,
                        int64_t n_atoms, int nframes, int64_t frame_stride, const double* scale,
-                       int flags, cudaStream_t st);
+                       int flags, cudaStream_t st, int slot = 0);
 int fused_plane_batch(const msf_plan* p, const void* grids, int grid_kind, int nframes, cudaStream_t st,
-                      int buf = 0);
+                      int buf = 0, int slot = 0);
 // alone: no plane FFT shares the SMs with this x pass (the last batch of a
 // chain, or a plan without overlap): the TMA x pass then fills every SM
 int fused_x_batch(const msf_plan* p, int nframes, double* sf, cudaStream_t st, int buf = 0, bool alone = true);

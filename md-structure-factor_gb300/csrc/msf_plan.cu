@@ -100,15 +100,18 @@ void plan_release(msf_plan* p) {
   for (int i = 0; i < 2; ++i) {
     if (p->ev_plane[i]) cudaEventDestroy(p->ev_plane[i]);
     if (p->ev_x[i]) cudaEventDestroy(p->ev_x[i]);
+    if (p->ev_bucket[i]) cudaEventDestroy(p->ev_bucket[i]);
     p->ev_plane[i] = nullptr;
     p->ev_x[i] = nullptr;
+    p->ev_bucket[i] = nullptr;
   }
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_plane_st) cudaEventDestroy(p->ev_plane_st);
   p->ev_fork = p->ev_plane_st = nullptr;
   if (p->side) cudaStreamDestroy(p->side);
   if (p->plane_st) cudaStreamDestroy(p->plane_st);
-  p->side = p->plane_st = nullptr;
+  if (p->bucket_st) cudaStreamDestroy(p->bucket_st);
+  p->side = p->plane_st = p->bucket_st = nullptr;
 }
 
 }  // namespace msf
@@ -246,6 +249,11 @@ int msf::plan_init(msf_plan* p, const msf_plan_desc* d) {
   p->off_poff = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * (n[0] + 1) * sizeof(int) : 0));
   p->off_pcount = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * n[0] * sizeof(int) : 0));
   p->off_pcursor = o; o = align_up(o + (variant == 3 ? (size_t)p->batch * n[0] * sizeof(int) : 0));
+  // with the overlap a second copy of the bucket arrays (off_offsets ..
+  // here), so that one batch's bucket sort can run beside the plane FFT of
+  // the batch before it
+  p->bk_delta = (variant == 3 && p->overlap) ? o - p->off_offsets : 0;
+  o += p->bk_delta;
   p->off_pnext = o; o = align_up(o + (variant == 3 ? sizeof(int) : 0));
   p->off_cplx = o; o = align_up(o + (size_t)p->batch * half_elems(p) * sizeof(float2));
   p->off_cplx2 = o; o = align_up(o + (p->overlap ? (size_t)p->batch * half_elems(p) * sizeof(float2) : 0));
@@ -294,18 +302,25 @@ int msf_plan_bind(msf_plan* p, void* ws, size_t bytes, msf_stream_t stream) {
     if (s) return s;
   } else {
     // per-plane counts start at zero; k_bucket_scan resets them after use
-    s = cuda_status(cudaMemsetAsync(p->ws + p->off_pcount, 0, (size_t)p->batch * p->n0 * sizeof(int), st));
+    for (int slot = 0; slot < (p->bk_delta ? 2 : 1) && !s; ++slot)
+      s = cuda_status(cudaMemsetAsync(p->ws + p->off_pcount + (slot ? p->bk_delta : 0), 0,
+                                      (size_t)p->batch * p->n0 * sizeof(int), st));
     if (s) return s;
   }
   if (p->overlap && !p->side) {
-    // two streams of equal (default) priority, whatever the caller's stream
-    // is (a legacy default stream, or one of raised priority that would give
-    // the plane FFTs precedence over the x passes)
+    // three streams, whatever the caller's stream is: the plane FFTs at the
+    // device's greatest priority, so that their persistent CTAs are placed
+    // first and the x passes and bucket sorts fill the room beside them; the
+    // x passes and bucket sorts at the default priority
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
-    if (cudaStreamCreateWithFlags(&p->plane_st, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
+    if (cudaStreamCreateWithPriority(&p->plane_st, cudaStreamNonBlocking, hi_prio) != cudaSuccess) return MSF_E_CUDA;
+    if (cudaStreamCreateWithFlags(&p->bucket_st, cudaStreamNonBlocking) != cudaSuccess) return MSF_E_CUDA;
     for (int i = 0; i < 2; ++i) {
       if (cudaEventCreateWithFlags(&p->ev_plane[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
       if (cudaEventCreateWithFlags(&p->ev_x[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
+      if (cudaEventCreateWithFlags(&p->ev_bucket[i], cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
     }
     if (cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
     if (cudaEventCreateWithFlags(&p->ev_plane_st, cudaEventDisableTiming) != cudaSuccess) return MSF_E_CUDA;
