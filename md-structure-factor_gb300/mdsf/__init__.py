@@ -14,13 +14,13 @@ plot2d.py:218-267), computed by hand-written sm_103a CUDA kernels in
 from . import _lib
 from ._lib import MsfError, load
 from .api import (DirectSF, cylindrical_average, direct_sf, ewald_from_sf, ewald_slices, get_dplot,
-                  hist_grid, plot_axes, power_accum, structure_factor)
+                  hist_grid, plot_axes, power_accum, release_staging, structure_factor)
 from .plan import Plan, get_plan
 from . import dens, synth, tune
 from .tune import tune_for
 
 __all__ = ["MsfError", "load", "DirectSF", "cylindrical_average", "direct_sf", "ewald_from_sf", "ewald_slices",
-           "get_dplot", "hist_grid", "plot_axes", "power_accum", "structure_factor", "Plan",
+           "get_dplot", "hist_grid", "plot_axes", "power_accum", "release_staging", "structure_factor", "Plan",
            "get_plan", "dens", "synth", "tune", "tune_for"]
 
 __version__ = "0.1.0"

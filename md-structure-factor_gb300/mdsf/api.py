@@ -14,6 +14,7 @@ is no CPU implementation behind any of them.
 from __future__ import annotations
 
 import math
+import threading
 
 import numpy as np
 import torch
@@ -78,6 +79,61 @@ def _side_stream(device):
         s = torch.cuda.Stream(device)
         _side_streams[device] = s
     return s
+
+
+class _Staging:
+    """The ring of device buffers host-streamed chunks are copied into, one
+    ring per device, kept across calls.  ``free[b]`` is an event recorded on
+    the caller's stream after the last chain that reads buffer b -- in this
+    call or an earlier one -- and every copy into b waits on it first, so a
+    call issued while an earlier call's kernels are still queued cannot
+    overwrite positions they have yet to bin.  (Per-call buffers from the
+    caching allocator cannot give that: a block freed at the end of one call
+    is handed to the next as soon as the copy stream is idle, while the
+    caller's stream may still be behind.)  Chunk i of a call takes slot
+    (turn + i) mod 3 and ``turn`` advances by the call's chunk count, so the
+    copies of a call issued back to back with the previous one (three chunks
+    each by default) wait on that call's chains one by one rather than on
+    its end.  The buffers are allocated on the copy stream and only grow;
+    :func:`release_staging` frees them."""
+
+    SLOTS = 3
+
+    def __init__(self):
+        self.bufs = [None] * self.SLOTS
+        self.free = [None] * self.SLOTS
+        self.turn = 0
+        self.lock = threading.Lock()
+
+    def view(self, b, side, shape, dtype):
+        """Buffer b as a `shape` tensor of `dtype`, grown if needed; call
+        on the copy stream after it has waited on ``free[b]``."""
+        nbytes = math.prod(shape) * torch.empty((), dtype=dtype).element_size()
+        buf = self.bufs[b]
+        if buf is None or buf.numel() < nbytes:
+            with torch.cuda.stream(side):
+                self.bufs[b] = None   # the old block returns to the copy stream's pool, behind the wait
+                buf = self.bufs[b] = torch.empty(nbytes, dtype=torch.uint8, device=side.device)
+        return buf[:nbytes].view(dtype).view(shape)
+
+
+_stagings = {}
+
+
+def release_staging(device=None):
+    """Free the host-streaming staging buffers of `device` (all devices if
+    None) once the kernels that read them have finished (the next streamed
+    call allocates them again)."""
+    for dev in ([_dev(device)] if device is not None else list(_stagings)):
+        stg = _stagings.pop(dev, None)
+        if stg is None:
+            continue
+        with stg.lock:
+            side = _side_stream(dev)
+            for ev in stg.free:
+                if ev is not None:
+                    side.wait_event(ev)
+            stg.bufs = [None] * stg.SLOTS
 
 
 _CHAIN = {4: "msf_hist_sf_f32", 3: "msf_hist_sf_f32xyz", 8: "msf_hist_sf_f64"}
@@ -201,29 +257,31 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
             side = _side_stream(device)
             # the short lead chunk pays only where the chunk calls overlap (bucketed plans)
             sizes = _chunk_sizes(T, chunk, lead=stream_chunk is None and plan.variant == 3)
-            bufs = [torch.empty((max(sizes), N, C), dtype=tdt, device=device) for _ in range(2)]
-            copied = [torch.cuda.Event() for _ in range(2)]
-            free = [None, None]
-            for b in bufs:
-                b.record_stream(side)
-            f0 = 0
-            for i, k in enumerate(sizes):
-                b = i % 2
-                with torch.cuda.stream(side):
-                    if free[b] is not None:
-                        side.wait_event(free[b])
-                    bufs[b][:k].copy_(hp[f0:f0 + k], non_blocking=True)
-                    copied[b].record(side)
-                main.wait_event(copied[b])
-                # one chain over the chunks: a bucketed plan's x pass of one
-                # chunk then overlaps the plane FFT of the next
-                more = MSF_CONTINUE if i + 1 < len(sizes) else 0
-                _launch_chain(plan, code, bufs[b].data_ptr(), wptr, N, k,
-                              scp + 24 * f0 if scp else 0, flags | more, sf, st)
-                ev = torch.cuda.Event()
-                ev.record(main)
-                free[b] = ev
-                f0 += k
+            copied = [torch.cuda.Event() for _ in range(_Staging.SLOTS)]
+            stg = _stagings.get(device)
+            if stg is None:
+                stg = _stagings[device] = _Staging()
+            with stg.lock:
+                f0 = 0
+                for i, k in enumerate(sizes):
+                    b = stg.turn % stg.SLOTS
+                    stg.turn += 1
+                    with torch.cuda.stream(side):
+                        if stg.free[b] is not None:
+                            side.wait_event(stg.free[b])
+                        buf = stg.view(b, side, (k, N, C), tdt)
+                        buf.copy_(hp[f0:f0 + k], non_blocking=True)
+                        copied[b].record(side)
+                    main.wait_event(copied[b])
+                    # one chain over the chunks: a bucketed plan's x pass of
+                    # one chunk then overlaps the plane FFT of the next
+                    more = MSF_CONTINUE if i + 1 < len(sizes) else 0
+                    _launch_chain(plan, code, buf.data_ptr(), wptr, N, k,
+                                  scp + 24 * f0 if scp else 0, flags | more, sf, st)
+                    ev = torch.cuda.Event()
+                    ev.record(main)
+                    stg.free[b] = ev
+                    f0 += k
     if mean and T > 0:
         sf.div_(T)
     return sf

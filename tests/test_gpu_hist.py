@@ -3,6 +3,7 @@
 Bar: the int32 grid is bit-exact with numpy.histogramdd; S(q) is within
 1e-5 * max(S) of the FP64 numpy path (FP32 FFT, FP64 frame sum)."""
 import os
+import time
 
 import numpy as np
 import pytest
@@ -140,6 +141,51 @@ def test_host_streamed_chunks(chunk):
                                 tuning=dict(batch=4), stream_chunk=chunk, zero_copy=False).cpu().numpy()
     assert mdsf.get_plan((64, 64, 32), box, max_atoms=4000, batch=4).tuning()["variant"] == "bucketed"
     assert rel_err(got, ref) < TOL
+
+
+def test_host_streamed_calls_back_to_back():
+    """Two host-streamed calls on different trajectories, issued back to
+    back without a synchronisation: each sf equals the same call run alone,
+    bit for bit (the second call's chunk copies must not overwrite staging
+    memory the first call's kernels have still to read)."""
+    dims, tun = (256, 256, 128), dict(batch=16)
+    a = [synth.columnar(frames=40, seed=s) for s in (21, 22)]
+    hs = [torch.from_numpy(synth.pack_float4(p, w)).pin_memory() for p, _, w in a]
+    box = a[0][1]
+    alone = []
+    for h in hs:
+        alone.append(mdsf.structure_factor(h, box, None, dims, tuning=tun))
+        torch.cuda.synchronize()
+    for _ in range(3):
+        got = [mdsf.structure_factor(h, box, None, dims, tuning=tun) for h in hs]
+        torch.cuda.synchronize()
+        for g, r in zip(got, alone):
+            assert torch.equal(g, r)
+
+
+def test_host_streamed_staging_outlives_a_stalled_stream():
+    """The caller's stream is held up (a sleep kernel) while a two-chunk
+    call's copies finish at once on the copy stream; a second call issued
+    then must not copy into staging memory the first call's kernels have
+    still to read: both results equal the calls run alone."""
+    dims, tun = (256, 256, 128), dict(batch=16)
+    a = [synth.columnar(frames=40, seed=s) for s in (31, 32)]
+    hs = [torch.from_numpy(synth.pack_float4(p, w)).pin_memory() for p, _, w in a]
+    box = a[0][1]
+    alone = []
+    for h in hs:
+        alone.append(mdsf.structure_factor(h, box, None, dims, tuning=tun, stream_chunk=20))
+        torch.cuda.synchronize()
+    torch.cuda._sleep(400_000_000)
+    first = mdsf.structure_factor(hs[0], box, None, dims, tuning=tun, stream_chunk=20)
+    time.sleep(0.05)
+    second = mdsf.structure_factor(hs[1], box, None, dims, tuning=tun, stream_chunk=20)
+    torch.cuda.synchronize()
+    assert torch.equal(first, alone[0])
+    assert torch.equal(second, alone[1])
+    mdsf.release_staging()
+    again = mdsf.structure_factor(hs[0], box, None, dims, tuning=tun, stream_chunk=20)
+    assert torch.equal(again, alone[0])
 
 
 @pytest.mark.parametrize("variant", [3, 4])
