@@ -86,6 +86,13 @@ __global__ void __launch_bounds__(XTmaShape<N0, W>::NT,
   constexpr int A = r2::Split2<N0>::A, B = r2::Split2<N0>::B;
   constexpr int ITEMS2 = B * W;
   constexpr int PER = (ITEMS2 + NT - 1) / NT;
+  // Rows narrower than 128 bytes (W < 16): the 32 / W k1 rows a warp reads
+  // in pass 2 sit A * W * 8 bytes apart, on the same banks.  Group
+  // g = k1 mod RG reads its A samples cyclically shifted by g rows, which
+  // spreads the groups over the banks; a cyclic shift of a DFT's input only
+  // multiplies each X[k] by a unit phase, so |X[k]|^2 is unchanged.
+  constexpr int RG = W * (int)sizeof(float2) < 128 ? (32 / W < A ? 32 / W : A) : 1;
+  static_assert((RG & (RG - 1)) == 0, "shift groups must be a power of two");
   float acc[PER][A];
 #pragma unroll
   for (int j = 0; j < PER; ++j)
@@ -117,10 +124,13 @@ __global__ void __launch_bounds__(XTmaShape<N0, W>::NT,
       const int it = j * NT + tid;
       if (ITEMS2 % NT == 0 || it < ITEMS2) {
         const int l = it % W, k1 = it / W;
+        const int g = k1 & (RG - 1);
         const float2* p = t + l + A * k1 * W;
+        const float2* q = p + g * W;
         float2 r[A];
 #pragma unroll
-        for (int n1 = 0; n1 < A; ++n1) r[n1] = p[n1 * W];
+        for (int n1 = 0; n1 < A; ++n1)   // sample (n1 + g) mod A; only the last RG - 1 can wrap
+          r[n1] = (n1 + RG - 1 < A || n1 + g < A) ? q[n1 * W] : q[(n1 - A) * W];
         reg::reg_dft<A>(r);
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = fmaf(r[k2].x, r[k2].x, fmaf(r[k2].y, r[k2].y, acc[j][k2]));
