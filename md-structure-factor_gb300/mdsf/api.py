@@ -255,7 +255,12 @@ def structure_factor(positions, box, weights=None, grid_dims=None, *, wrap=False
                 hp = hp.contiguous().pin_memory()
             main = torch.cuda.current_stream(device)
             side = _side_stream(device)
-            # the short lead chunk pays only where the chunk calls overlap (bucketed plans)
+            # the short lead chunk pays only where the chunk calls overlap
+            # (bucketed plans): 7% of an isolated 100-frame call against two
+            # 50-frame chunks, and a tie back to back (42.5k against 42.4k
+            # frames/s, interleaved on one GB300).  The chunks set the chain's
+            # batches and so the rounding of the FP32 frame sums: the split
+            # depends on the call's sizes only, never on the GPU's state.
             sizes = _chunk_sizes(T, chunk, lead=stream_chunk is None and plan.variant == 3)
             copied = [torch.cuda.Event() for _ in range(_Staging.SLOTS)]
             stg = _stagings.get(device)
