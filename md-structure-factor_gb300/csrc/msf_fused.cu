@@ -244,9 +244,15 @@ __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
     __stcs(out + q * NH + k, cadd(E, t));   // evict-first: keep L2 for the bucket entries
     __stcs(out + (q + P) * NH + k, csub(E, t));
   };
+  // Odd passes over the units take their slots rotated by 32 within each k1
+  // block (a bijection there, as NT is a multiple of H): an edge unit's extra
+  // emits serialise its warp, and with two passes of NT threads (the
+  // headline shape) every warp then holds one edge unit instead of the even
+  // warps two and the odd ones none.
+  constexpr bool ROT = H % 64 == 0 && NT % H == 0;
   for (int u = threadIdx.x; u < U; u += NT) {
     int l, lp, k1, k1p;
-    const int kk = u / H, ll = u % H;
+    const int kk = u / H, ll = ROT ? (u + ((u / NT) & 1) * 32) % H : u % H;
     const bool edge = ll == 0;
     if (edge) {                      // edge line: k1 = 0 pairs the two self-paired items
       l = lp = kk < B / 2 ? 0 : N2 / 2;

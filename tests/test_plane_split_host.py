@@ -13,11 +13,19 @@ PLANES = [(32, 32), (64, 32), (128, 32), (256, 32), (512, 32), (32, 64), (64, 64
           (32, 128), (64, 128), (128, 128), (256, 128), (32, 256), (64, 256), (128, 256)]
 
 
+def threads(n1, n2):
+    """PlaneShape::NT."""
+    return 512 if n2 * (n1 // 2) >= 4096 else 256
+
+
 def units(n1, n2):
     B, A = SPLIT2[n1 // 2]
     H = n2 // 2
+    NT = threads(n1, n2)
+    rot = H % 64 == 0 and NT % H == 0   # odd passes rotated by 32 within each k1 block
     for u in range(B * H):
-        kk, ll = divmod(u, H)
+        kk = u // H
+        ll = (u + ((u // NT) & 1) * 32) % H if rot else u % H
         if ll == 0:
             l = lp = 0 if kk < B // 2 else n2 // 2
             k1 = kk % (B // 2)
@@ -67,3 +75,19 @@ def test_twiddle_index_uniform_per_warp():
         us = list(units(n1, n2))
         for w in range(0, len(us), 32):
             assert len({u // (n2 // 2) for u, *_ in us[w:w + 32]}) == 1
+
+
+@pytest.mark.parametrize("n1,n2", [(256, 128), (128, 128), (64, 256)])
+def test_edge_units_spread_over_warps(n1, n2):
+    """With the odd passes rotated, no warp holds more edge units than the
+    passes it makes need: at the headline shape (two passes) one per warp."""
+    NT = threads(n1, n2)
+    per_warp = {}
+    for u, edge, *_ in units(n1, n2):
+        if edge:
+            w = (u % NT) // 32
+            per_warp[w] = per_warp.get(w, 0) + 1
+    B, _ = SPLIT2[n1 // 2]
+    assert max(per_warp.values()) == -(-B // (NT // 32))
+    if (n1, n2) == (256, 128):
+        assert sorted(per_warp) == list(range(16)) and set(per_warp.values()) == {1}
