@@ -6,10 +6,12 @@
 // cp.async.bulk.tensor.2d into one of NS shared-memory buffers and tracked by
 // an mbarrier, so the copies of items s+1 .. s+NS-1 run while item s is
 // transformed (NS = 2: four buffers per 16 KB tile measured slower alone, as
-// they cost half the CTAs per SM).  Tiles of at most 2048 values take
-// 128-thread CTAs: beside a plane-FFT CTA (the overlapped launch) two of
-// them fit, alone six per SM.  x-FFT (DIF, natural input, output at pos(k)),
-// |F|^2 summed over the frames of the tile in FP32, one FP64
+// they cost half the CTAs per SM).  A CTA has 16 values of a tile per
+// thread: 2048-value tiles take 128-thread CTAs (two beside a plane-FFT CTA
+// in the overlapped launch, six per SM alone), larger ones 256.  (4-column
+// tiles on four 64-thread CTAs beside the plane CTA measured slower: 8.3
+// against 6.7 us per frame for the 256-point x pass alone, 32-byte box
+// rows.)  x-FFT (DIF, natural input, output at pos(k)), |F|^2 summed over the frames of the tile in FP32, one FP64
 // read-modify-write of sf per tile every kPowerFlush frames and after the
 // last.  Waits are bounded: on timeout the kernel latches MSF_E_TIMEOUT in
 // the plan status word and returns.
@@ -30,7 +32,8 @@ struct XTmaArgs {
 
 template <int N0, int W>
 struct XTmaShape {
-  static constexpr int NT = N0 * W >= 4096 ? 256 : 128;
+  // 16 values per thread, 64 to 256 threads
+  static constexpr int NT = N0 * W / 16 < 64 ? 64 : (N0 * W / 16 > 256 ? 256 : N0 * W / 16);
   static constexpr int EPT = N0 * W / NT;
   static constexpr int BOX_ROWS = N0 <= 256 ? N0 : 256;
   static constexpr int NBOX = N0 / BOX_ROWS;
@@ -88,10 +91,13 @@ __global__ void __launch_bounds__(XTmaShape<N0, W>::NT,
   constexpr int PER = (ITEMS2 + NT - 1) / NT;
   // Rows narrower than 128 bytes (W < 16): the 32 / W k1 rows a warp reads
   // in pass 2 sit A * W * 8 bytes apart, on the same banks.  Group
-  // g = k1 mod RG reads its A samples cyclically shifted by g rows, which
-  // spreads the groups over the banks; a cyclic shift of a DFT's input only
-  // multiplies each X[k] by a unit phase, so |X[k]|^2 is unchanged.
-  constexpr int RG = W * (int)sizeof(float2) < 128 ? (32 / W < A ? 32 / W : A) : 1;
+  // g = k1 mod RG reads its A samples cyclically shifted by g rows, RG the
+  // rows per 128 bytes, which spreads the groups evenly over the banks (two
+  // wavefronts per 256-byte access, the least there is); a cyclic shift of a
+  // DFT's input only multiplies each X[k] by a unit phase, so |X[k]|^2 is
+  // unchanged.
+  constexpr int RW = 128 / (W * (int)sizeof(float2));
+  constexpr int RG = RW > 1 ? (RW < A ? RW : A) : 1;
   static_assert((RG & (RG - 1)) == 0, "shift groups must be a power of two");
   float acc[PER][A];
 #pragma unroll
@@ -216,8 +222,8 @@ static int launch_xtma(const msf_plan* p, const CUtensorMap* map, const XTmaArgs
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_xpower_tma<N0, W>, S::NT, S::SMEM);
     grid = (sms > 0 ? sms : 152) * (occ > 0 ? occ : 1);
   }
-  // beside a plane FFT: one 256-thread or two 128-thread CTAs per SM (they
-  // co-reside with the plane CTA); alone: as many as fit
+  // beside a plane FFT: 256 threads of x-pass CTAs per SM (they co-reside
+  // with the plane CTA); alone: as many as fit
   const int cap = (p->overlap && !alone) ? (sms > 0 ? sms : 152) * (256 / S::NT) : grid;
   const int g = a.ntiles < cap ? a.ntiles : cap;
   k_xpower_tma<N0, W><<<g, S::NT, S::SMEM, st>>>(*map, a);
