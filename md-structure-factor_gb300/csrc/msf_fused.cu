@@ -659,13 +659,21 @@ static int x_ct(const XCtArgs& a, int n0, int w, cudaStream_t st) {
 }
 
 // the requested tile width if it is instantiated for n0, else (0) the widest
-// tile of at most 4096 complex values (32 KB: two fit beside the plane FFT)
+// tile of at most 2048 complex values -- the TMA x pass then runs two
+// 128-thread CTAs beside a plane-FFT CTA, measured faster than one 256-thread
+// CTA of 4096-value tiles beside it and alone (256-point lines: 6.68 against
+// 7.45 us per frame alone, 44.8k against 44.2k frames/s for the chain) --
+// or the narrowest instantiated when every tile is larger
 int ct_x_width(int n0, int requested) {
-  int best = 0;
-#define X(A, B) if (n0 == A && (requested == 0 ? (B > best && A * B <= 4096) : B == requested)) best = B;
+  int best = 0, narrow = 0;
+#define X(A, B)                                                               \
+  if (n0 == A) {                                                              \
+    if (requested ? B == requested : (A * B <= 2048 && B > best)) best = B;   \
+    if (!narrow || B < narrow) narrow = B;                                    \
+  }
   MSF_X_CASES(X)
 #undef X
-  return best;
+  return best || requested ? best : narrow;
 }
 
 // w_N^k = exp(-2 pi i k/N) rounded to float: cos/sin in double of the angle

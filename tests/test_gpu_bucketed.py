@@ -126,8 +126,12 @@ def test_too_many_atoms_for_the_plan():
 
 
 def test_headline_plan_uses_tma_x_pass():
+    """The default x tile of 256-point lines: 8 columns (2048 values, two
+    128-thread CTAs beside the plane FFT)."""
     plan = mdsf.get_plan((256, 256, 128), (16.0, 13.856, 8.0), max_atoms=1000, variant=3, batch=4)
-    assert plan.tma and plan.tile_w == 16
+    assert plan.tma and plan.tile_w == 8
+    for dims, w in (((128, 64, 32), 16), ((64, 64, 64), 32), ((512, 64, 64), 8)):
+        assert mdsf.get_plan(dims, (1.0, 1.0, 1.0), max_atoms=1000, variant=3, batch=2).tile_w == w, dims
 
 
 @pytest.mark.parametrize("dims", [(64, 64, 64), (128, 64, 32), (256, 32, 64)])
