@@ -39,12 +39,27 @@ struct SmZArgs {
   const float2* tw; // w_n2^k
 };
 
+// cp.async of 8 bytes (src_bytes 0: zero fill, nothing read)
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int src_bytes) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ float load_any(const void* g, int kind, int64_t i) {
   if (kind == kGridI32) return load_grid<kGridI32>(g, i);
   if (kind == kGridF32) return load_grid<kGridF32>(g, i);
   return load_grid<kGridF64>(g, i);
 }
 
+// (16-byte loads of eight z per lane with the lanes over lines, which keeps
+// the shared-memory stores conflict-free, measured 4.3x slower: 1.46 ms
+// against 0.34 ms for 8 frames of 192^3 -- each warp load then touches 32
+// rows, and every load is followed by the zeroing store of the same bytes)
 // three CTAs per SM (80 registers) for the 512-point lines, which used 94
 // registers (two CTAs per SM) on their own: the 512^3 stress grid went from
 // 562 to 600-700 frames/s.  The other lengths keep the compiler's choice
@@ -142,17 +157,40 @@ struct SmXArgs {
   const float2* tw; // w_n0^k
 };
 
+// tile buffers of k_xs: two, filled by cp.async (frame b + 1's copy runs
+// while frame b is transformed: 8 frames of 192^3 0.130 -> 0.073 ms, the
+// batched systems 35.2k -> 37.0k frames/s) where they fit in 96 KB, else one
+// filled through registers -- the 512-point lines keep two CTAs per SM (128
+// registers, 70 KB): double-buffered, at one CTA per SM, the 512^3 stress
+// grid fell from 709 to 550 frames/s.  The other lengths
+// take no block bound (0): the compiler's own choice keeps them at 70-127
+// registers, where a bound of one block took the 192-point lines from 71 to
+// 137 (two CTAs per SM instead of three)
+__host__ __device__ constexpr int xs_bufs(int n0) { return 2 * n0 * kSmoothW * 8 <= 96 * 1024 ? 2 : 1; }
+
 template <int N0>
-__global__ void __launch_bounds__(kSmoothThreads) k_xs(SmXArgs a) {
+__global__ void __launch_bounds__(kSmoothThreads, xs_bufs(N0) == 1 ? 2 : 0) k_xs(SmXArgs a) {
   constexpr int W = kSmoothW, NT = kSmoothThreads;
   constexpr int A = mixed::Split2m<N0>::A, B = mixed::Split2m<N0>::B;
   constexpr int I2 = B * W, PER = (I2 + NT - 1) / NT;
   extern __shared__ __align__(16) float2 smem[];
-  float2* tile = smem;             // [N0][W]
-  float2* tw = tile + N0 * W;      // N0
+  constexpr int NB = xs_bufs(N0);
+  float2* tiles = smem;            // NB [N0][W] tiles: frame b in tile b % NB
+  float2* tw = tiles + NB * N0 * W; // N0
   const int64_t f0 = (int64_t)blockIdx.x * W;
   const int weff = (int)min((int64_t)W, a.F - f0);
   copy_table(tw, a.tw, N0);
+  // frame b's tile by cp.async (columns past F filled with zeros)
+  auto fetch = [&](int b) {
+    const float2* src = a.C + b * a.Vh + f0;
+    float2* dst = tiles + (b % NB) * (N0 * W);
+    for (int e = threadIdx.x; e < N0 * W; e += NT) {
+      const int x = e / W, w = e % W;
+      cp_async8(dst + e, src + (int64_t)x * a.F + (w < weff ? w : 0), w < weff ? 8 : 0);
+    }
+    cp_async_commit();
+  };
+  if (NB == 2 && a.nframes > 0) fetch(0);
   // pass-2 items (k1, column l) owned by this thread: X[k1 + B k2] in acc
   float acc[PER][A];
 #pragma unroll
@@ -160,16 +198,25 @@ __global__ void __launch_bounds__(kSmoothThreads) k_xs(SmXArgs a) {
 #pragma unroll
     for (int k = 0; k < A; ++k) acc[j][k] = 0.f;
   for (int b = 0; b < a.nframes; ++b) {
-    const float2* src = a.C + b * a.Vh + f0;
-    __syncthreads();   // the previous frame's pass 2 is done with the tile
-    gather_batched<8, float2>(
-        N0 * W,
-        [&](int e) {
-          const int x = e / W, w = e % W;
-          return w < weff ? __ldg(src + (int64_t)x * a.F + w) : make_float2(0.f, 0.f);
-        },
-        [&](int e, float2 v) { tile[e] = v; });
-    __syncthreads();
+    // two buffers: tile (b + 1) % 2 was frame b - 1's, which every thread
+    // has finished (the barrier at the end of the previous iteration)
+    if constexpr (NB == 1) {   // the register gather (128 registers, no spill)
+      const float2* src = a.C + b * a.Vh + f0;
+      gather_batched<8, float2>(
+          N0 * W,
+          [&](int e) {
+            const int x = e / W, w = e % W;
+            return w < weff ? __ldg(src + (int64_t)x * a.F + w) : make_float2(0.f, 0.f);
+          },
+          [&](int e, float2 v) { tiles[e] = v; });
+    } else if (b + 1 < a.nframes) {
+      fetch(b + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();   // every thread's copies of frame b have landed
+    float2* tile = tiles + (b % NB) * (N0 * W);
     mixed::pass1<N0, W, W, 1, NT>(tile, tw);
     __syncthreads();
 #pragma unroll
@@ -202,6 +249,7 @@ __global__ void __launch_bounds__(kSmoothThreads) k_xs(SmXArgs a) {
         for (int k2 = 0; k2 < A; ++k2) acc[j][k2] = 0.f;
       }
     }
+    __syncthreads();   // frame b's tile is free for frame b + NB
   }
 }
 
@@ -250,7 +298,7 @@ int launch_ys(const msf_plan* p, int nframes, cudaStream_t st) {
 
 template <int N0>
 int launch_xs(const msf_plan* p, int nframes, double* sf, cudaStream_t st) {
-  const size_t smem = ((size_t)N0 * kSmoothW + N0) * sizeof(float2);
+  const size_t smem = ((size_t)xs_bufs(N0) * N0 * kSmoothW + N0) * sizeof(float2);
   static bool once = false;
   allow_smem_once(k_xs<N0>, once, smem);
   SmXArgs a;
