@@ -76,6 +76,8 @@ __global__ void __launch_bounds__(kSmoothThreads, zs_min_blocks(N2)) k_zs(SmZArg
   const int64_t p0 = (int64_t)blockIdx.x * G;
   copy_table(tw, a.tw, N2);
   void* gw = const_cast<void*>(a.grids);
+  // 8 elements (16 loads) in flight per thread (12, at the same three CTAs
+  // per SM, measured 3% slower on the batched systems)
   gather_batched<8, float2>(
       G * N2,
       [&](int e) {
