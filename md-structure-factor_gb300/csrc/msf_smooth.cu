@@ -132,10 +132,10 @@ __global__ void __launch_bounds__(kSmoothThreads, zs_min_blocks(N2)) k_zs(SmZArg
   zs_fft_split<N2, G>(buf, tw, a, frame, p0);
 }
 
-// Row pairs per CTA of the bulk-copied z sweep (lines of at most 256
-// points): the line buffer plus the block's raw rows (8 G n2 bytes) fit two
-// (n2 = 160..192) or three times per SM.
-__host__ __device__ constexpr int bulk_rows(int n2) { return n2 <= 192 ? 32 : 16; }
+// Row pairs per CTA of the bulk-copied z sweep: the line buffer plus the
+// block's raw rows (8 G n2 bytes) fit two (n2 = 160..192) or three times
+// per SM.
+__host__ __device__ constexpr int bulk_rows(int n2) { return n2 <= 192 ? 32 : (n2 <= 256 ? 16 : 8); }
 template <int N2>
 constexpr size_t zs_bulk_smem() {
   return (size_t)N2 * (bulk_rows(N2) + 2) * sizeof(float2) + (size_t)2 * bulk_rows(N2) * N2 * sizeof(int32_t);
@@ -373,7 +373,7 @@ int launch_zs(const msf_plan* p, const void* grids, int kind, int nframes, int z
   a.tw = ws_ptr<float2>(p, p->off_tw[2]);
   a.status = ws_ptr<int>(p, p->off_status);
   const int64_t pairs = (a.rows + 1) / 2;
-  if constexpr (N2 <= 256) {
+  {
     // int32 grids whose frames start 16-byte aligned take the bulk copies
     if (kind == kGridI32 && reinterpret_cast<uintptr_t>(grids) % 16 == 0 && a.V % 4 == 0) {
       constexpr int GB = bulk_rows(N2);
