@@ -137,16 +137,19 @@ __global__ void __launch_bounds__(kSmoothThreads, zs_min_blocks(N2)) k_zs(SmZArg
 // per SM.
 __host__ __device__ constexpr int bulk_rows(int n2) { return n2 <= 192 ? 32 : (n2 <= 256 ? 16 : 8); }
 template <int N2>
-constexpr size_t zs_bulk_smem() {
-  return (size_t)N2 * (bulk_rows(N2) + 2) * sizeof(float2) + (size_t)2 * bulk_rows(N2) * N2 * sizeof(int32_t);
+constexpr size_t zs_bulk_smem() {   // line buffer, twiddles, raw rows + 4 ints of alignment slack
+  return (size_t)N2 * (bulk_rows(N2) + 2) * sizeof(float2) + ((size_t)2 * bulk_rows(N2) * N2 + 4) * sizeof(int32_t);
 }
 
-// k_zs for int32 grids at 16-byte aligned frames: the CTA's 2G rows are
+// k_zs for int32 grids at a 16-byte aligned base: the CTA's 2G rows are
 // contiguous in the grid, so one cp.async.bulk copy (mbarrier, bounded wait)
 // brings them into shared memory -- tens of KB in flight per CTA instead of
-// 16 scalar loads per thread -- (a tail of fewer than four ints by plain
-// loads), the block is zeroed by 16-byte stores behind the copy, and the
-// rows are transposed into the line buffer from shared memory.
+// 16 scalar loads per thread --, the block is zeroed by 16-byte stores
+// behind the copy, and the rows are transposed into the line buffer from
+// shared memory.  The block sits in shared memory at its misalignment
+// (0-3 ints) so that its 16-byte aligned interior lands aligned there too;
+// the fewer than four ints before and after the interior move by plain
+// loads and stores, so nothing outside the block is read or written.
 template <int N2>
 __global__ void __launch_bounds__(kSmoothThreads) k_zs_bulk(SmZArgs a) {
   constexpr int G = bulk_rows(N2), S = G + 1, NT = kSmoothThreads;
@@ -160,9 +163,13 @@ __global__ void __launch_bounds__(kSmoothThreads) k_zs_bulk(SmZArgs a) {
   const int frame = blockIdx.y;
   const int64_t p0 = (int64_t)blockIdx.x * G, r0 = 2 * p0;
   const int nrows = (int)min((int64_t)2 * G, a.rows - r0);
-  int32_t* src = static_cast<int32_t*>(const_cast<void*>(a.grids)) + frame * a.V + r0 * N2;
-  const int n = nrows * N2;   // ints of the block
-  const int nb = n & ~3;      // the bulk-copied part: a multiple of 16 bytes
+  const int64_t first = frame * a.V + r0 * N2;   // int index of the block
+  int32_t* src = static_cast<int32_t*>(const_cast<void*>(a.grids)) + first;
+  const int n = nrows * N2;                       // ints of the block
+  const int off = (int)(first & 3);               // its misalignment; block int i at raw[off + i]
+  const int hn = min(off ? 4 - off : 0, n);       // ints before the aligned interior
+  const int nb = (n - hn) & ~3;                   // the bulk-copied interior: a multiple of 16 bytes
+  const int tn = n - hn - nb;                     // ints after it (0-3)
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     failed = 0;
@@ -171,9 +178,10 @@ __global__ void __launch_bounds__(kSmoothThreads) k_zs_bulk(SmZArgs a) {
   __syncthreads();
   if (threadIdx.x == 0 && nb > 0) {
     mbar_expect_tx(&bar, (uint32_t)nb * 4u);
-    bulk_copy_g2s(raw, src, (uint32_t)nb * 4u, &bar);
+    bulk_copy_g2s(raw + off + hn, src + hn, (uint32_t)nb * 4u, &bar);
   }
-  if (threadIdx.x < n - nb) raw[nb + threadIdx.x] = __ldcg(src + nb + threadIdx.x);
+  if (threadIdx.x < hn) raw[off + threadIdx.x] = __ldcg(src + threadIdx.x);
+  if (threadIdx.x < tn) raw[off + hn + nb + threadIdx.x] = __ldcg(src + hn + nb + threadIdx.x);
   copy_table(tw, a.tw, N2);
   if (nb > 0) {
     long long spins = 0;
@@ -194,14 +202,16 @@ __global__ void __launch_bounds__(kSmoothThreads) k_zs_bulk(SmZArgs a) {
     return;
   }
   if (a.zero) {   // the copy has landed: nothing reads these bytes any more
-    int4* z4 = reinterpret_cast<int4*>(src);
+    int4* z4 = reinterpret_cast<int4*>(src + hn);
     for (int i = threadIdx.x; i < nb / 4; i += NT) z4[i] = make_int4(0, 0, 0, 0);
-    if (threadIdx.x < n - nb) src[nb + threadIdx.x] = 0;
+    if (threadIdx.x < hn) src[threadIdx.x] = 0;
+    if (threadIdx.x < tn) src[hn + nb + threadIdx.x] = 0;
   }
+  const int32_t* rb = raw + off;
   for (int e = threadIdx.x; e < G * N2; e += NT) {
     const int g = e / N2, z = e - g * N2;
-    const float va = 2 * g < nrows ? (float)raw[2 * g * N2 + z] : 0.f;
-    const float vb = 2 * g + 1 < nrows ? (float)raw[(2 * g + 1) * N2 + z] : 0.f;
+    const float va = 2 * g < nrows ? (float)rb[2 * g * N2 + z] : 0.f;
+    const float vb = 2 * g + 1 < nrows ? (float)rb[(2 * g + 1) * N2 + z] : 0.f;
     buf[z * S + g] = make_float2(va, vb);
   }
   __syncthreads();
@@ -374,8 +384,8 @@ int launch_zs(const msf_plan* p, const void* grids, int kind, int nframes, int z
   a.status = ws_ptr<int>(p, p->off_status);
   const int64_t pairs = (a.rows + 1) / 2;
   {
-    // int32 grids whose frames start 16-byte aligned take the bulk copies
-    if (kind == kGridI32 && reinterpret_cast<uintptr_t>(grids) % 16 == 0 && a.V % 4 == 0) {
+    // int32 grids at a 16-byte aligned base take the bulk copies
+    if (kind == kGridI32 && reinterpret_cast<uintptr_t>(grids) % 16 == 0) {
       constexpr int GB = bulk_rows(N2);
       static bool once_b = false;
       allow_smem_once(k_zs_bulk<N2>, once_b, zs_bulk_smem<N2>());
