@@ -7,13 +7,18 @@
 // (one exchange through shared memory per pass) instead of one pass per
 // radix stage with runtime index arithmetic.
 //
-//   k_zs<n2>  G row pairs (y = 2p, 2p+1 of the flattened (x, y) rows) per CTA,
+//   k_zs_bulk<n2>, k_zs<n2>
+//             G row pairs (y = 2p, 2p+1 of the flattened (x, y) rows) per CTA,
 //             read from the int32 grid (which is zeroed behind the read) as
-//             x[2p] + i x[2p+1], z-FFT, split into the two rows' half spectra
+//             x[2p] + i x[2p+1], z-FFT, split into the two rows' half
+//             spectra; the rows arrive by one bulk copy per CTA (k_zs_bulk)
+//             or by register-staged loads (float grids, unaligned bases)
 //   k_ys<n1>  (x, W kz columns) per CTA: y-FFT in place in the spectra
-//   k_xs<n0>  W (y, kz) columns per CTA: x-FFT of every frame of the batch,
-//             |F|^2 summed in FP32 in registers, one FP64 RMW of sf every
-//             kPowerFlush frames and after the last
+//   k_xs<n0>  W (y, kz) columns per CTA: x-FFT of every frame of the batch
+//             (the next frame's tile copied by cp.async under the current
+//             one's transform where two tiles fit), |F|^2 summed in FP32 in
+//             registers, one FP64 RMW of sf every kPowerFlush frames and
+//             after the last
 #include "msf_mixed.cuh"
 #include "msf_tma.cuh"
 
@@ -85,14 +90,16 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                : "memory");
 }
 
+// k_zs: the register-staged z sweep, for float grids and int32 grids at a
+// base that is not 16-byte aligned (k_zs_bulk below takes the others).
+// Three CTAs per SM (80 registers) for the 512-point lines, which used 94
+// registers (two CTAs per SM) on their own: the 512^3 stress grid went from
+// 562 to 600-700 frames/s.  The other lengths keep the compiler's choice
+// (the same bound on the 256-point lines cost the batched systems 4%).
 // (16-byte loads of eight z per lane with the lanes over lines, which keeps
 // the shared-memory stores conflict-free, measured 4.3x slower: 1.46 ms
 // against 0.34 ms for 8 frames of 192^3 -- each warp load then touches 32
-// rows, and every load is followed by the zeroing store of the same bytes)
-// three CTAs per SM (80 registers) for the 512-point lines, which used 94
-// registers (two CTAs per SM) on their own: the 512^3 stress grid went from
-// 562 to 600-700 frames/s.  The other lengths keep the compiler's choice
-// (the same bound on the 256-point lines cost the batched systems 4%)
+// rows, and every load is followed by the zeroing store of the same bytes.)
 __host__ __device__ constexpr int zs_min_blocks(int n2) { return n2 == 512 ? 3 : 1; }
 
 template <int N2>
