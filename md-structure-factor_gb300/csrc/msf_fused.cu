@@ -227,7 +227,9 @@ struct PlaneShape {
 // it the twiddle index w^q, q = k1 + B*k2 -- is uniform across a warp when
 // n2/2 is a multiple of 32 (one constant-cache access per twiddle), and the
 // B slots with l = 0 hold the 2 x B/2 edge units (line 0 for k1 < B/2, line
-// n2/2 for the others), one per warp pair instead of all in warp 0.
+// n2/2 for the others), spread over the warps instead of all in warp 0 (one
+// per warp at the headline shape, with the rotation of the odd passes
+// below).
 template <int N1, int N2, int SP, int NT, bool ZERO = false, bool PAIRS = false>
 __device__ __forceinline__ void ypass2_split(float2* buf, float2* out) {
   constexpr int P = N1 / 2, NH = N2 / 2 + 1;
