@@ -76,7 +76,8 @@ typedef struct msf_plan_desc {
                              memory by the plane FFT kernel (power-of-two grids),
                              4 smooth: three sweeps with compile-time mixed-radix FFTs
                              (every axis 2^a 3^b 5^c in 16..256, or 512) */
-  int32_t tile_w;         /* columns per x-pass tile: 0 auto, else 4..32 */
+  int32_t tile_w;         /* columns per x-pass tile: 0 auto (variant 3: the widest tile of
+                             at most 2048 values, 8 columns for 256-point lines), else 4..32 */
   int32_t rows_per_block; /* row pairs per z-pass block: 0 auto */
   int32_t deposit_block;  /* threads per deposit block: 0 auto */
   int64_t max_atoms;      /* atoms per frame the chain may be called with (sizes the per-plane
